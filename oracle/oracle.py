@@ -1,0 +1,202 @@
+"""Python face of the FP64 CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, by `__graft_entry__.smoke()` and by bench.py's CPU-baseline
+leg (and its `--impl reference` arm) -- as the checker, never by the product
+package.  Wraps oracle/_build/liborc.so (a C++ restatement of the reference's
+Float64 dense path, see bem_oracle.cpp) and adds the dense solve the
+reference runs through LinearSolve.jl -> OpenBLAS LU
+(src/Core/LinearSolveUtils.jl:44-49), here SciPy's LAPACK getrf/getrs.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liborc.so")
+
+NEARFIELD = {"tanp3c": 0, "plain": 1, "euclid": 2, "csinh": 3, "sinhsinh": 4, "tangent": 5, "p3c": 6}
+
+
+class OrcGeom(ctypes.Structure):
+    _fields_ = [("nt", ctypes.c_int32), ("n", ctypes.c_int32), ("ne", ctypes.c_int32),
+                ("p", ctypes.c_int32), ("ngeo", ctypes.c_int32)] + [
+        (nm, ctypes.POINTER(ctypes.c_double))
+        for nm in ("px", "py", "nx", "ny", "jac", "elen", "gx", "gy", "ew")]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        d = ctypes.c_double
+        P = ctypes.POINTER(d)
+        i = ctypes.c_int
+        _lib.orc_assemble.argtypes = [ctypes.POINTER(OrcGeom), i, d, d, i, d, i, i, i, P, P]
+        _lib.orc_assemble.restype = i
+        _lib.orc_integrate_element.argtypes = [ctypes.POINTER(OrcGeom), i, d, d, i, i, i, i, d, d, i, P, P]
+        _lib.orc_near_mask.argtypes = [ctypes.POINTER(OrcGeom), d, ctypes.POINTER(ctypes.c_uint8)]
+        _lib.orc_gausslegendre.argtypes = [i, P, P]
+        _lib.orc_shapefun.argtypes = [i, i, d, P, P]
+        _lib.orc_closest_point_1d.argtypes = [i, i, P, d, d, P, P, P]
+        _lib.orc_complex_pole_1d.argtypes = [i, i, P, d, d, P, P]
+        _lib.orc_map.argtypes = [i, P, P, i, d, d, P, P]
+        _lib.orc_map.restype = i
+        _lib.orc_sinh_map.argtypes = [P, i, d, d, P, P]
+        _lib.orc_eq40_AB.argtypes = [d, P, P, P]
+        _lib.orc_p3c_inv_pole.argtypes = [d, d, P, P]
+        _lib.orc_interp_rule.argtypes = [d, i, P, P, P, P]
+        _lib.orc_interp_rule.restype = i
+        FN = ctypes.CFUNCTYPE(d, d)
+        _lib.FN = FN
+        _lib.orc_laurent_coefficients_interp.argtypes = [FN, d, i, i, P]
+        _lib.orc_laurent_coefficients_interp.restype = i
+        _lib.orc_guiggiani_integral_interp.argtypes = [FN, d, i, i]
+        _lib.orc_guiggiani_integral_interp.restype = d
+        _lib.orc_guiggiani_GH_interp.argtypes = [FN, FN, d, i, i, i, P, P]
+        _lib.orc_laplace_kernel.argtypes = [d, d, d, d, d, P, P]
+        _lib.orc_kelvin_kernel.argtypes = [d, d, d, d, d, d, P, P]
+        _lib.orc_near_element.argtypes = [P, i, d, d, d, d]
+        _lib.orc_near_element.restype = i
+        _lib.orc_apply_bc.argtypes = [ctypes.c_int64, ctypes.c_int64, P, P,
+                                      ctypes.POINTER(ctypes.c_int32), P, P, P]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_geom(dad):
+    """Pack a BEMdata into the oracle's struct; returns (struct, keepalive)."""
+    keep = dict(
+        px=np.ascontiguousarray(dad.collocation[:, 0]), py=np.ascontiguousarray(dad.collocation[:, 1]),
+        nx=np.ascontiguousarray(dad.normal[:, 0]), ny=np.ascontiguousarray(dad.normal[:, 1]),
+        jac=np.ascontiguousarray(dad.jacobian), elen=np.ascontiguousarray(dad.elem_length),
+        gx=np.ascontiguousarray(dad.geo[..., 0].reshape(-1)) if dad.ngeo else np.zeros(1),
+        gy=np.ascontiguousarray(dad.geo[..., 1].reshape(-1)) if dad.ngeo else np.zeros(1),
+        ew=np.ascontiguousarray(dad.elem_weight))
+    g = OrcGeom(dad.nt, dad.n, dad.ne, dad.p, dad.ngeo, *[_p(keep[k]) for k in
+                ("px", "py", "nx", "ny", "jac", "elen", "gx", "gy", "ew")])
+    return g, keep
+
+
+def _props(dad):
+    pr = dad.properties
+    if pr.ndof == 1:
+        return 0, float(pr.k), 0.0
+    return 1, float(pr.mu), float(pr.nu_eff)
+
+
+def assemble(dad, npg=20, near_factor=1.5, nearfield="tanp3c", singular="guiggiani", threads=0,
+             store=True):
+    """Dense FP64 H, G (H_G_full_direct, src/Core/Assembly_full.jl:61-175)."""
+    L = lib()
+    g, keep = make_geom(dad)
+    kind, a, b = _props(dad)
+    rows = dad.ndof * dad.nt
+    cols = dad.ndof * dad.n
+    H = np.zeros((rows, rows), order="F")
+    G = np.zeros((rows, cols), order="F")
+    rc = L.orc_assemble(ctypes.byref(g), kind, a, b, npg, float(near_factor), NEARFIELD[nearfield],
+                        1 if singular == "telles" else 0, threads, _p(H), _p(G))
+    if rc != 0:
+        raise ValueError(f"oracle assemble failed ({rc})")
+    if store:
+        dad.set_cache(H=H, G=G)
+    return H, G
+
+
+def integrate_element(dad, e, pf, source=-1, npg=20, nearfield="tanp3c", singular="guiggiani"):
+    L = lib()
+    g, keep = make_geom(dad)
+    kind, a, b = _props(dad)
+    nc = 1 if kind == 0 else 4
+    h = np.zeros((dad.p + 1) * nc)
+    gg = np.zeros((dad.p + 1) * nc)
+    L.orc_integrate_element(ctypes.byref(g), kind, a, b, npg, NEARFIELD[nearfield],
+                            1 if singular == "telles" else 0, e, float(pf[0]), float(pf[1]),
+                            int(source), _p(h), _p(gg))
+    return h, gg
+
+
+def near_mask(dad, near_factor=1.5):
+    L = lib()
+    g, keep = make_geom(dad)
+    m = np.zeros((dad.nt, dad.ne), np.uint8)
+    L.orc_near_mask(ctypes.byref(g), float(near_factor), m.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    return m
+
+
+def apply_bc(dad, H=None, G=None):
+    """Column swap into A x = b (src/Core/Boundary_conditions.jl:54-75, 152-174)."""
+    H = dad.cache["H"] if H is None else H
+    G = dad.cache["G"] if G is None else G
+    rows, cols = G.shape
+    A = np.zeros((rows, rows), order="F")
+    b = np.zeros(rows)
+    BC = np.ascontiguousarray(dad.BC, dtype=np.int32)
+    BV = np.ascontiguousarray(dad.BV, dtype=np.float64)
+    lib().orc_apply_bc(rows, cols, _p(np.asfortranarray(H)), _p(np.asfortranarray(G)),
+                       BC.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _p(BV), _p(A), _p(b))
+    return A, b
+
+
+def lu_solve(A, b):
+    """Dense LU with partial pivoting (LAPACK getrf/getrs through SciPy)."""
+    import scipy.linalg as sla
+    lu, piv = sla.lu_factor(A, overwrite_a=False, check_finite=False)
+    return sla.lu_solve((lu, piv), b, check_finite=False)
+
+
+def split_sol(dad, x):
+    """Scatter x into (T, q) or (u, traction) (src/Core/Solver.jl:88-98, 133-146)."""
+    BC, BV = dad.BC, dad.BV
+    if dad.ndof == 1:
+        T = np.array(x[: dad.nt], dtype=np.float64)
+        q = np.zeros(dad.n)
+        d = BC == 0
+        q[d] = T[: dad.n][d]
+        T[: dad.n][d] = BV[d]
+        q[~d] = BV[~d]
+        dad.set_cache(T=T, q=q, x=np.asarray(x))
+        return T
+    nb = 2 * dad.n
+    u = np.where(BC == 0, BV, x[:nb])
+    t = np.where(BC == 0, x[:nb], BV)
+    dad.set_cache(u=u, traction=t, T=u, x=np.asarray(x))
+    return u
+
+
+def solve(dad):
+    """applyBC + LU solve + split (src/Core/Solver.jl:24-64, 114-131)."""
+    A, b = apply_bc(dad)
+    x = lu_solve(A, b)
+    dad.set_cache(A=A, b=b)
+    return split_sol(dad, x)
+
+
+def timed_pipeline(dad, npg=16, threads=0):
+    """assemble + applyBC + LU + split, wall-clock seconds per stage."""
+    t0 = time.perf_counter()
+    assemble(dad, npg=npg, threads=threads)
+    t1 = time.perf_counter()
+    A, b = apply_bc(dad)
+    t2 = time.perf_counter()
+    x = lu_solve(A, b)
+    t3 = time.perf_counter()
+    split_sol(dad, x)
+    return dict(assemble=t1 - t0, apply_bc=t2 - t1, lu=t3 - t2, total=t3 - t0, x=x)
