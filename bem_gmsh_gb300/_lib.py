@@ -1,0 +1,130 @@
+"""ctypes binding of libbem_gb300.so (the C ABI declared in include/bem_gb300.h).
+
+There is no CPU fallback: if the library is missing or no CUDA device is
+present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _build
+
+BEM_OK = 0
+BEM_F32, BEM_F64 = 32, 64
+BEM_MEM_HOST, BEM_MEM_DEVICE = 0, 1
+BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
+          4: "refinement did not converge", 5: "device wait timed out", 6: "unsupported"}
+
+D = ctypes.c_double
+PD = ctypes.POINTER(ctypes.c_double)
+I32 = ctypes.c_int32
+I64 = ctypes.c_int64
+VP = ctypes.c_void_p
+
+
+class BemGeom2D(ctypes.Structure):
+    _fields_ = [("nt", I32), ("n", I32), ("ne", I32), ("p", I32), ("ngeo", I32), ("reserved", I32),
+                ("px", VP), ("py", VP), ("nx", VP), ("ny", VP), ("jac", VP), ("elen", VP),
+                ("geo_x", VP), ("geo_y", VP), ("elem_weight", VP)]
+
+
+class BemSolveStats(ctypes.Structure):
+    _fields_ = [("status", I32), ("iterations", I32), ("rel_residual", D), ("t_assemble_ms", D),
+                ("t_factor_ms", D), ("t_refine_ms", D)]
+
+
+class BemError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the shared library (building it first only if asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise BemError(f"{_build.LIB} is missing: run __graft_entry__.build() first")
+        _build.build()
+    L = ctypes.CDLL(_build.LIB)
+    ctx_p = ctypes.c_void_p
+    sig = {
+        "bem_ctx_create": ([ctypes.c_int, ctypes.POINTER(ctx_p)], ctypes.c_int),
+        "bem_ctx_destroy": ([ctx_p], ctypes.c_int),
+        "bem_ctx_set_stream": ([ctx_p, VP], ctypes.c_int),
+        "bem_last_error": ([ctx_p], ctypes.c_char_p),
+        "bem_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "bem_assemble_laplace2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, ctypes.c_int, D, ctypes.c_int,
+                                    ctypes.c_int, VP, I64, VP, I64], ctypes.c_int),
+        "bem_assemble_kelvin2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, D, ctypes.c_int, D, ctypes.c_int,
+                                   ctypes.c_int, VP, I64, VP, I64], ctypes.c_int),
+        "bem_assemble_system2d": ([ctx_p, ctypes.POINTER(BemGeom2D), ctypes.c_int, D, D, VP, VP,
+                                   ctypes.c_int, D, ctypes.c_int, VP, I64, VP], ctypes.c_int),
+    }
+    optional = {
+        "bem_solve2d": ([ctx_p, ctypes.POINTER(BemGeom2D), ctypes.c_int, D, D, VP, VP, ctypes.c_int, D,
+                         ctypes.c_int, D, ctypes.c_int, ctypes.c_int, VP, ctypes.POINTER(BemSolveStats)],
+                        ctypes.c_int),
+        "bem_solve_system": ([ctx_p, I64, VP, I64, VP, ctypes.c_int, D, ctypes.c_int, ctypes.c_int, VP,
+                              ctypes.POINTER(BemSolveStats)], ctypes.c_int),
+    }
+    for name, (args, res) in {**sig, **optional}.items():
+        if not hasattr(L, name):
+            if name in sig:
+                raise BemError(f"{_build.LIB} does not export {name}")
+            continue
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+class Context:
+    """One device, one stream, cached device workspace (bem_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        self.h = ctypes.c_void_p()
+        rc = self.L.bem_ctx_create(device, ctypes.byref(self.h))
+        if rc != BEM_OK:
+            raise BemError(f"bem_ctx_create({device}) failed: {STATUS.get(rc, rc)}")
+
+    def check(self, rc: int, what: str):
+        if rc != BEM_OK:
+            msg = self.L.bem_last_error(self.h).decode()
+            raise BemError(f"{what}: {STATUS.get(rc, rc)} {msg}".strip())
+
+    def set_stream(self, stream_ptr: int):
+        self.check(self.L.bem_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")
+
+    def close(self):
+        if self.h:
+            self.L.bem_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = {}
+
+
+def default_context(device: int = 0) -> Context:
+    c = _default_ctx.get(device)
+    if c is None:
+        c = _default_ctx[device] = Context(device)
+    return c

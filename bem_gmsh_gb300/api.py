@@ -1,0 +1,154 @@
+"""Host-side mirror of the reference's user API for the dense path.
+
+    dad = quadrado(ndiv=20)                    # format2d equivalent
+    assemble(dad, 20, method="gpu")            # assemble!(dad, npg; method=:gpu)
+    solve(dad)                                 # solve(dad) -> dad.T, dad.q
+    rel_error(dad)
+
+Reference: `assemble!` (src/Core/Assembly_full.jl:107-118), `H_G_gpu`
+(src/Laplace/Assembly_GPU.jl:120-150, src/Elasticity/Assembly_GPU.jl:15-51),
+`solve` (src/Core/Solver.jl:24-64, 114-131).  Every call goes through the C
+ABI of libbem_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from .geometry import BEMdata, Laplace, Elasticity
+
+_KEEP = "_bem_keepalive"
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def geom_struct(dad: BEMdata, device: bool = False):
+    """Pack a BEMdata into the C struct `bem_geom2d`.
+
+    device=False: host numpy arrays (BEM_MEM_HOST).  device=True: the arrays
+    are copied once to CUDA tensors (BEM_MEM_DEVICE).  Returns (struct, keep)
+    where `keep` holds the arrays alive."""
+    arrs = dict(
+        px=np.ascontiguousarray(dad.collocation[:, 0], dtype=np.float64),
+        py=np.ascontiguousarray(dad.collocation[:, 1], dtype=np.float64),
+        nx=np.ascontiguousarray(dad.normal[:, 0], dtype=np.float64),
+        ny=np.ascontiguousarray(dad.normal[:, 1], dtype=np.float64),
+        jac=np.ascontiguousarray(dad.jacobian, dtype=np.float64),
+        elen=np.ascontiguousarray(dad.elem_length, dtype=np.float64),
+        gx=np.ascontiguousarray(dad.geo[..., 0].reshape(-1), dtype=np.float64),
+        gy=np.ascontiguousarray(dad.geo[..., 1].reshape(-1), dtype=np.float64),
+        ew=np.ascontiguousarray(dad.elem_weight, dtype=np.float64))
+    if device:
+        import torch
+        arrs = {k: torch.from_numpy(v).cuda() for k, v in arrs.items()}
+        ptr = {k: (v.data_ptr() if v.numel() else None) for k, v in arrs.items()}
+    else:
+        ptr = {k: (v.ctypes.data if v.size else None) for k, v in arrs.items()}
+    g = _lib.BemGeom2D(dad.nt, dad.n, dad.ne, dad.p, dad.ngeo, 0, ptr["px"], ptr["py"], ptr["nx"],
+                       ptr["ny"], ptr["jac"], ptr["elen"], ptr["gx"], ptr["gy"], ptr["ew"])
+    return g, arrs
+
+
+def _ptr(x):
+    if _is_torch(x):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+def _ld(x) -> int:
+    """Leading dimension of a column-major 2-D array / tensor."""
+    if _is_torch(x):
+        s = x.stride()
+        assert s[0] == 1, "expected column-major (Fortran-ordered) storage"
+        return s[1] if x.shape[1] > 1 else x.shape[0]
+    assert x.flags.f_contiguous, "expected a Fortran-ordered array"
+    return x.shape[0]
+
+
+def H_G_gpu(dad: BEMdata, T=np.float32, npg: int = 20, near: str = "cpu", near_factor: float = 1.5,
+            device: str = "cuda", out=None, ctx: _lib.Context | None = None, store: bool = True):
+    """Dense H, G on the GPU (reference `H_G_gpu`).
+
+    T: np.float32 (far field in FP32, near/singular FP64) or np.float64.
+    near: "cpu" in the reference means near/singular entries by
+    `integrate_element`; here they are computed on the GPU in FP64, so "cpu"
+    and "gpu" are both accepted and give the full near correction.
+    device must be "cuda" (no CPU fallback).  `out=(H, G)` may pass
+    preallocated column-major numpy arrays or CUDA tensors."""
+    if device != "cuda":
+        raise ValueError("device must be 'cuda'; this build has no CPU path")
+    if near not in ("cpu", "gpu"):
+        raise ValueError(f"near must be 'cpu' or 'gpu'; got {near!r}")
+    T = np.dtype(T)
+    if T not in (np.float32, np.float64):
+        raise ValueError(f"H_G_gpu T must be float32 or float64; got {T}")
+    ctx = ctx or _lib.default_context()
+    pr = dad.properties
+    dof = pr.ndof
+    rows, gcols = dof * dad.nt, dof * dad.n
+    dev = False
+    if out is None:
+        H = np.zeros((rows, rows), dtype=T, order="F")
+        G = np.zeros((rows, gcols), dtype=T, order="F")
+    else:
+        H, G = out
+        dev = _is_torch(H)
+    g, keep = geom_struct(dad, device=dev)
+    mem = _lib.BEM_MEM_DEVICE if dev else _lib.BEM_MEM_HOST
+    dt = _lib.BEM_F32 if T == np.float32 else _lib.BEM_F64
+    if isinstance(pr, Laplace):
+        rc = ctx.L.bem_assemble_laplace2d(ctx.h, g, float(pr.k), int(npg), float(near_factor), dt, mem,
+                                          _ptr(H), _ld(H), _ptr(G), _ld(G))
+    elif isinstance(pr, Elasticity):
+        rc = ctx.L.bem_assemble_kelvin2d(ctx.h, g, float(pr.mu), float(pr.nu_eff), int(npg),
+                                         float(near_factor), dt, mem, _ptr(H), _ld(H), _ptr(G), _ld(G))
+    else:
+        raise ValueError(f"H_G_gpu supports Laplace and Elasticity; got {type(pr).__name__}")
+    ctx.check(rc, "H_G_gpu")
+    if store:
+        dad.set_cache(H=H, G=G)
+    return H, G
+
+
+def assemble(dad: BEMdata, npg: int = 20, method: str = "gpu", **kw):
+    """`assemble!(dad, npg; method)` for the GPU method."""
+    if method != "gpu":
+        raise ValueError("this package provides method='gpu' only")
+    return H_G_gpu(dad, npg=npg, **kw)
+
+
+def assemble_system(dad: BEMdata, npg: int = 20, near_factor: float = 1.5, out=None,
+                    ctx: _lib.Context | None = None):
+    """Assembly with `applyBC`'s column swap fused: FP64 A, b."""
+    ctx = ctx or _lib.default_context()
+    pr = dad.properties
+    dof = pr.ndof
+    rows = dof * dad.nt
+    if out is None:
+        A = np.zeros((rows, rows), order="F")
+        b = np.zeros(rows)
+        dev = False
+        BC = np.ascontiguousarray(dad.BC, dtype=np.int32)
+        BV = np.ascontiguousarray(dad.BV, dtype=np.float64)
+    else:
+        A, b = out
+        dev = _is_torch(A)
+        if dev:
+            import torch
+            BC = torch.as_tensor(np.asarray(dad.BC, np.int32)).cuda()
+            BV = torch.as_tensor(np.asarray(dad.BV, np.float64)).cuda()
+        else:
+            BC = np.ascontiguousarray(dad.BC, dtype=np.int32)
+            BV = np.ascontiguousarray(dad.BV, dtype=np.float64)
+    g, keep = geom_struct(dad, device=dev)
+    kind = 0 if isinstance(pr, Laplace) else 1
+    p0 = float(pr.k) if kind == 0 else float(pr.mu)
+    p1 = 0.0 if kind == 0 else float(pr.nu_eff)
+    rc = ctx.L.bem_assemble_system2d(ctx.h, g, kind, p0, p1, _ptr(BC), _ptr(BV), int(npg),
+                                     float(near_factor),
+                                     _lib.BEM_MEM_DEVICE if dev else _lib.BEM_MEM_HOST, _ptr(A), _ld(A),
+                                     _ptr(b))
+    ctx.check(rc, "assemble_system")
+    return A, b

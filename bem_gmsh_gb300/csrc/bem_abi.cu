@@ -1,0 +1,420 @@
+// C-ABI layer: context, workspace, argument checks, host<->device staging.
+// The entry points are declared (with the reference interfaces they replace)
+// in include/bem_gb300.h.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bem_gb300.h"
+#include "bem_abi_internal.h"
+#include "bem_kernels.h"
+
+using bem::AsmRequest;
+using bem::GeomDev;
+using bem::Physics;
+using bem::Rules;
+
+// ---------------------------------------------------------------------------
+// host-side rule tables
+// ---------------------------------------------------------------------------
+namespace {
+
+// Gauss-Legendre nodes (ascending) and weights: Newton on the three-term
+// recurrence in extended precision.
+void gauss_legendre(int n, double* x, double* w) {
+  const int m = (n + 1) / 2;
+  for (int i = 0; i < m; ++i) {
+    long double z = std::cos(3.14159265358979323846L * (i + 0.75L) / (n + 0.5L));
+    long double pp = 0;
+    for (int it = 0; it < 100; ++it) {
+      long double p1 = 1, p2 = 0;
+      for (int j = 1; j <= n; ++j) {
+        long double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1);
+      long double z1 = z;
+      z = z1 - p1 / pp;
+      if ((double)z == (double)z1 && it > 2) break;
+    }
+    long double p1 = 1, p2 = 0;
+    for (int j = 1; j <= n; ++j) {
+      long double p3 = p2;
+      p2 = p1;
+      p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
+    }
+    pp = n * (z * p1 - p2) / (z * z - 1);
+    x[n - 1 - i] = (double)z;
+    x[i] = -(double)z;
+    w[i] = w[n - 1 - i] = (double)(2.0L / ((1 - z * z) * pp * pp));
+  }
+  if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+// differentiation matrix of a barycentric basis (Interpolation.jl:193-213)
+void diff_matrix(const double* x, const double* bw, int n, double* D) {
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      double t = (bw[j] / bw[i]) / (x[i] - x[j]);
+      D[i * n + j] = t;
+      s += t;
+    }
+    D[i * n + i] = -s;
+  }
+}
+
+void build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) {
+  std::memset(&R, 0, sizeof(R));
+  const int nn = g->p + 1;
+  R.nn = nn;
+  R.ngeo = g->ngeo;
+  R.npg = npg;
+  // Legendre(p): Gauss nodes, weights (2 isodd(i) - 1) sqrt((1 - x^2) w)
+  double x[64], w[64];
+  gauss_legendre(nn, x, w);
+  for (int i = 0; i < nn; ++i) {
+    R.leg_x[i] = x[i];
+    R.leg_bw[i] = ((i % 2) == 0 ? 1.0 : -1.0) * std::sqrt((1 - x[i] * x[i]) * w[i]);
+  }
+  diff_matrix(R.leg_x, R.leg_bw, nn, R.leg_D);
+  // Equispaced(ngeo-1): nodes (2j-N)/N, weights (-1)^(j+N) binomial(N, j)
+  if (g->ngeo > 0) {
+    const int N = g->ngeo - 1;
+    double binom = 1.0;
+    for (int j = 0; j <= N; ++j) {
+      if (j > 0) binom = std::round(binom * (N - j + 1) / j);
+      R.geo_x[j] = N == 0 ? 0.0 : (double)(2 * j - N) / (double)N;
+      bool pos = ((N % 2) == 1) != ((j % 2) == 0);
+      R.geo_bw[j] = (pos ? 1.0 : -1.0) * binom;
+    }
+    diff_matrix(R.geo_x, R.geo_bw, g->ngeo, R.geo_D);
+  }
+  gauss_legendre(npg, R.qsi, R.w);
+  gauss_legendre(BEM_NINTERP, R.gi_x, R.gi_w);
+  for (int i = 0; i < BEM_NINTERP; ++i) {
+    double b = 1.0;
+    for (int j = 0; j < BEM_NINTERP; ++j)
+      if (j != i) b *= R.gi_x[i] - R.gi_x[j];
+    R.gi_bw[i] = 1.0 / b;
+  }
+  for (int k = 0; k < nn; ++k) R.ew[k] = ew_host[k];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+void* bem_ctx::get(int slot, size_t bytes) {
+  Buf& b = slots[slot];
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return b.p;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  size_t want = bytes + bytes / 8;
+  if (cudaMalloc(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return nullptr;
+  }
+  b.bytes = want;
+  return b.p;
+}
+
+int bem_ctx::cuda_fail(cudaError_t e, const char* where) {
+  last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? BEM_ERR_NOMEM : BEM_ERR_CUDA;
+}
+
+extern "C" int bem_ctx_create(int device, bem_ctx** out) {
+  if (!out) return BEM_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return BEM_ERR_INVALID;
+  }
+  bem_ctx* c = new bem_ctx();
+  c->device = device;
+  cudaSetDevice(device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BEM_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return BEM_OK;
+}
+
+extern "C" int bem_ctx_destroy(bem_ctx* c) {
+  if (!c) return BEM_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& b : c->slots)
+    if (b.p) cudaFree(b.p);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return BEM_OK;
+}
+
+extern "C" int bem_ctx_set_stream(bem_ctx* c, void* s) {
+  if (!c) return BEM_ERR_INVALID;
+  c->stream = s ? (cudaStream_t)s : c->own_stream;
+  return BEM_OK;
+}
+
+extern "C" const char* bem_last_error(bem_ctx* c) { return c ? c->last_error.c_str() : ""; }
+
+extern "C" const char* bem_status_string(int s) {
+  switch (s) {
+    case BEM_OK: return "ok";
+    case BEM_ERR_INVALID: return "invalid argument";
+    case BEM_ERR_CUDA: return "CUDA error";
+    case BEM_ERR_NOMEM: return "device out of memory";
+    case BEM_ERR_NOT_CONVERGED: return "refinement did not converge";
+    case BEM_ERR_INTERNAL: return "device wait timed out";
+    case BEM_ERR_UNSUPPORTED: return "unsupported size or degree";
+    default: return "unknown status";
+  }
+}
+
+// ---------------------------------------------------------------------------
+// geometry staging
+// ---------------------------------------------------------------------------
+int bem_check_geom(const bem_geom2d* g, int npg, double near_factor) {
+  if (!g) return BEM_ERR_INVALID;
+  if (g->p < 1 || g->p + 1 > BEM_MAXNN) return BEM_ERR_UNSUPPORTED;
+  if (g->ngeo < 0 || g->ngeo == 1 || g->ngeo > BEM_MAXGEO) return BEM_ERR_UNSUPPORTED;
+  if (g->ne <= 0 || g->n != g->ne * (g->p + 1) || g->nt < g->n) return BEM_ERR_INVALID;
+  if (npg < 1 || npg > BEM_MAXNPG) return BEM_ERR_UNSUPPORTED;
+  if (!(near_factor > 0)) return BEM_ERR_INVALID;
+  if (!g->px || !g->py || !g->nx || !g->ny || !g->jac || !g->elen || !g->elem_weight)
+    return BEM_ERR_INVALID;
+  if (g->ngeo > 0 && (!g->geo_x || !g->geo_y)) return BEM_ERR_INVALID;
+  // pair indices and column offsets are 32-bit
+  if ((int64_t)g->nt * 2 >= (int64_t)1 << 30) return BEM_ERR_UNSUPPORTED;
+  return BEM_OK;
+}
+
+int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& gd, Rules& R) {
+  const int nn = g->p + 1;
+  double ew[BEM_MAXNN];
+  if (mem == BEM_MEM_HOST) {
+    std::memcpy(ew, g->elem_weight, sizeof(double) * nn);
+  } else {
+    if (cudaMemcpy(ew, g->elem_weight, sizeof(double) * nn, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return c->cuda_fail(cudaGetLastError(), "elem_weight");
+  }
+  build_rules(g, npg, ew, R);
+  gd.nt = g->nt;
+  gd.n = g->n;
+  gd.ne = g->ne;
+  gd.nn = nn;
+  gd.ngeo = g->ngeo;
+  if (mem == BEM_MEM_DEVICE) {
+    gd.px = g->px; gd.py = g->py; gd.nx = g->nx; gd.ny = g->ny;
+    gd.jac = g->jac; gd.elen = g->elen; gd.gx = g->geo_x; gd.gy = g->geo_y;
+    return BEM_OK;
+  }
+  const size_t ng = (size_t)g->ne * g->ngeo;
+  const size_t tot = 2 * (size_t)g->nt + 3 * (size_t)g->n + (size_t)g->ne + 2 * ng;
+  double* d = (double*)c->get(bem_ctx::SLOT_GEOM, tot * sizeof(double));
+  if (!d) return BEM_ERR_NOMEM;
+  size_t o = 0;
+  auto put = [&](const double* src, size_t cnt) -> const double* {
+    double* dst = d + o;
+    if (cnt) cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    o += cnt;
+    return dst;
+  };
+  gd.px = put(g->px, g->nt);
+  gd.py = put(g->py, g->nt);
+  gd.nx = put(g->nx, g->n);
+  gd.ny = put(g->ny, g->n);
+  gd.jac = put(g->jac, g->n);
+  gd.elen = put(g->elen, g->ne);
+  gd.gx = ng ? put(g->geo_x, ng) : nullptr;
+  gd.gy = ng ? put(g->geo_y, ng) : nullptr;
+  return BEM_OK;
+}
+
+// Runs one assembly (device pointers already set in q), retrying once with
+// a larger pair list if the first estimate overflowed.
+int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
+  const int nt = q.g.nt;
+  const int dof = q.ph.kind == 0 ? 1 : 2;
+  q.rows = (float4*)c->get(bem_ctx::SLOT_ROWS, sizeof(float4) * (size_t)nt);
+  q.nodes = (bem::NodeRec*)c->get(bem_ctx::SLOT_NODES, sizeof(bem::NodeRec) * (size_t)q.g.n);
+  q.elems = (bem::ElemRec*)c->get(bem_ctx::SLOT_ELEMS, sizeof(bem::ElemRec) * (size_t)q.g.ne);
+  q.rowsum = (double*)c->get(bem_ctx::SLOT_ROWSUM, sizeof(double) * (size_t)nt * dof * dof);
+  q.gdiag = (double*)c->get(bem_ctx::SLOT_GDIAG, sizeof(double) * (size_t)q.g.n * dof * dof);
+  q.counters = (int*)c->get(bem_ctx::SLOT_COUNTERS, 64);
+  q.absmax = (unsigned long long*)((char*)q.counters + 32);
+  if (!q.rows || !q.nodes || !q.elems || !q.rowsum || !q.gdiag || !q.counters) return BEM_ERR_NOMEM;
+  int cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : nt * 16 + 4096;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    q.pairs = (int2*)c->get(bem_ctx::SLOT_PAIRS, sizeof(int2) * (size_t)cap);
+    if (!q.pairs) return BEM_ERR_NOMEM;
+    q.pair_cap = cap;
+    int rc = bem::launch_assembly(q, c->stream);
+    if (rc != 0) return c->cuda_fail((cudaError_t)rc, "launch_assembly");
+    int hc[2] = {0, 0};
+    cudaMemcpyAsync(hc, q.counters, sizeof(hc), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "assembly");
+    if (hc[1] != 0) {
+      c->last_error = "bulk-copy wait timed out in the far-field kernel";
+      return BEM_ERR_INTERNAL;
+    }
+    if (hc[0] <= cap) {
+      c->pair_cap_hint = std::max(c->pair_cap_hint, hc[0] + hc[0] / 4 + 1024);
+      return BEM_OK;
+    }
+    cap = hc[0] + hc[0] / 4 + 1024;
+  }
+  return BEM_ERR_INTERNAL;
+}
+
+// ---------------------------------------------------------------------------
+// H, G assembly
+// ---------------------------------------------------------------------------
+static int assemble_hg(bem_ctx* c, const bem_geom2d* g, const Physics& ph, int npg, double nf,
+                       int dtype, int mem, void* H, int64_t ldh, void* G, int64_t ldg) {
+  if (!c) return BEM_ERR_INVALID;
+  int rc = bem_check_geom(g, npg, nf);
+  if (rc) return rc;
+  if (dtype != BEM_F32 && dtype != BEM_F64) return BEM_ERR_INVALID;
+  if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  const int dof = ph.kind == 0 ? 1 : 2;
+  const int64_t rows = (int64_t)dof * g->nt, hcols = rows, gcols = (int64_t)dof * g->n;
+  if (!H || !G || ldh < rows || ldg < rows) return BEM_ERR_INVALID;
+  cudaSetDevice(c->device);
+  AsmRequest q{};
+  rc = bem_stage_geom(c, g, npg, mem, q.g, q.R);
+  if (rc) return rc;
+  q.ph = ph;
+  q.near_factor = nf;
+  q.prec = dtype == BEM_F32 ? 0 : 1;
+  q.fused = 0;
+  const size_t esz = dtype == BEM_F32 ? 4 : 8;
+  if (mem == BEM_MEM_DEVICE) {
+    q.H = H; q.ld = ldh; q.G = G; q.ldg = ldg;
+  } else {
+    const int64_t ldp = (rows + 3) / 4 * 4;
+    q.H = c->get(bem_ctx::SLOT_OUT0, esz * (size_t)ldp * hcols);
+    q.G = c->get(bem_ctx::SLOT_OUT1, esz * (size_t)ldp * gcols);
+    if (!q.H || !q.G) return BEM_ERR_NOMEM;
+    q.ld = q.ldg = ldp;
+  }
+  rc = bem_run_assembly(c, q);
+  if (rc) return rc;
+  if (mem == BEM_MEM_HOST) {
+    cudaMemcpy2DAsync(H, esz * ldh, q.H, esz * q.ld, esz * rows, hcols, cudaMemcpyDeviceToHost,
+                      c->stream);
+    cudaMemcpy2DAsync(G, esz * ldg, q.G, esz * q.ldg, esz * rows, gcols, cudaMemcpyDeviceToHost,
+                      c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "copy H, G to host");
+  }
+  return BEM_OK;
+}
+
+extern "C" int bem_assemble_laplace2d(bem_ctx* c, const bem_geom2d* g, double k, int npg,
+                                      double nf, int dtype, int mem, void* H, int64_t ldh, void* G,
+                                      int64_t ldg) {
+  if (!(k > 0) || !std::isfinite(k)) return BEM_ERR_INVALID;
+  Physics ph{};
+  ph.kind = 0;
+  ph.k = k;
+  return assemble_hg(c, g, ph, npg, nf, dtype, mem, H, ldh, G, ldg);
+}
+
+extern "C" int bem_assemble_kelvin2d(bem_ctx* c, const bem_geom2d* g, double mu, double nu,
+                                     int npg, double nf, int dtype, int mem, void* H, int64_t ldh,
+                                     void* G, int64_t ldg) {
+  if (!(mu > 0) || !(nu < 0.5) || !(nu > -1.0)) return BEM_ERR_INVALID;
+  Physics ph{};
+  ph.kind = 1;
+  ph.mu = mu;
+  ph.nu = nu;
+  return assemble_hg(c, g, ph, npg, nf, dtype, mem, H, ldh, G, ldg);
+}
+
+// ---------------------------------------------------------------------------
+// fused system assembly
+// ---------------------------------------------------------------------------
+int bem_assemble_system_dev(bem_ctx* c, const bem_geom2d* g, const Physics& ph, const int32_t* BC,
+                            const double* BV, int npg, double nf, int mem, int prec, double* A,
+                            int64_t lda, float* A32, double* b) {
+  int rc = bem_check_geom(g, npg, nf);
+  if (rc) return rc;
+  const int dof = ph.kind == 0 ? 1 : 2;
+  const int64_t nb = (int64_t)dof * g->n;
+  cudaSetDevice(c->device);
+  AsmRequest q{};
+  rc = bem_stage_geom(c, g, npg, mem, q.g, q.R);
+  if (rc) return rc;
+  q.ph = ph;
+  q.near_factor = nf;
+  q.prec = prec;
+  q.fused = 1;
+  if (mem == BEM_MEM_HOST) {
+    int32_t* dbc = (int32_t*)c->get(bem_ctx::SLOT_BC, sizeof(int32_t) * (size_t)nb);
+    double* dbv = (double*)c->get(bem_ctx::SLOT_BV, sizeof(double) * (size_t)nb);
+    if (!dbc || !dbv) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(dbc, BC, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dbv, BV, sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream);
+    q.bc = dbc;
+    q.bv = dbv;
+  } else {
+    q.bc = BC;
+    q.bv = BV;
+  }
+  q.H = A;
+  q.ld = lda;
+  q.G = nullptr;
+  q.ldg = lda;
+  q.A32 = A32;
+  q.b = b;
+  return bem_run_assembly(c, q);
+}
+
+extern "C" int bem_assemble_system2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm0,
+                                     double prm1, const int32_t* BC, const double* BV, int npg,
+                                     double nf, int mem, double* A, int64_t lda, double* b) {
+  if (!c || !g || !BC || !BV || !A || !b) return BEM_ERR_INVALID;
+  if (kind != 0 && kind != 1) return BEM_ERR_INVALID;
+  if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  Physics ph{};
+  ph.kind = kind;
+  if (kind == 0) {
+    if (!(prm0 > 0)) return BEM_ERR_INVALID;
+    ph.k = prm0;
+  } else {
+    if (!(prm0 > 0) || !(prm1 < 0.5) || !(prm1 > -1.0)) return BEM_ERR_INVALID;
+    ph.mu = prm0;
+    ph.nu = prm1;
+  }
+  const int dof = kind == 0 ? 1 : 2;
+  const int64_t rows = (int64_t)dof * g->nt;
+  if (lda < rows) return BEM_ERR_INVALID;
+  if (mem == BEM_MEM_DEVICE)
+    return bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, 1, A, lda, nullptr, b);
+  const int64_t ldp = (rows + 3) / 4 * 4;
+  double* dA = (double*)c->get(bem_ctx::SLOT_OUT0, sizeof(double) * (size_t)ldp * rows);
+  double* db = (double*)c->get(bem_ctx::SLOT_OUT1, sizeof(double) * (size_t)rows);
+  if (!dA || !db) return BEM_ERR_NOMEM;
+  int rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, 1, dA, ldp, nullptr, db);
+  if (rc) return rc;
+  cudaMemcpy2DAsync(A, 8 * lda, dA, 8 * ldp, 8 * rows, rows, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(b, db, 8 * rows, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "copy A, b to host");
+  return BEM_OK;
+}

@@ -1,0 +1,41 @@
+// Context object and helpers shared by the C-ABI translation units.
+#pragma once
+#include <algorithm>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/bem_gb300.h"
+#include "bem_kernels.h"
+
+struct bem_ctx {
+  enum Slot {
+    SLOT_GEOM, SLOT_ROWS, SLOT_NODES, SLOT_ELEMS, SLOT_ROWSUM, SLOT_GDIAG, SLOT_COUNTERS,
+    SLOT_PAIRS, SLOT_BC, SLOT_BV, SLOT_OUT0, SLOT_OUT1, SLOT_OUT2, SLOT_OUT3,
+    SLOT_LU0, SLOT_LU1, SLOT_LU2, SLOT_LU3, SLOT_LU4, SLOT_LU5, SLOT_LU6, SLOT_LU7,
+    NSLOT
+  };
+  struct Buf {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  Buf slots[NSLOT];
+  int pair_cap_hint = 0;
+
+  // Grow-only device buffer for `slot` (NULL on allocation failure).
+  void* get(int slot, size_t bytes);
+  int cuda_fail(cudaError_t e, const char* where);
+};
+
+int bem_check_geom(const bem_geom2d* g, int npg, double near_factor);
+int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, bem::GeomDev& gd,
+                   bem::Rules& R);
+int bem_run_assembly(bem_ctx* c, bem::AsmRequest& q);
+int bem_assemble_system_dev(bem_ctx* c, const bem_geom2d* g, const bem::Physics& ph,
+                            const int32_t* BC, const double* BV, int npg, double nf, int mem,
+                            int prec, double* A, int64_t lda, float* A32, double* b);

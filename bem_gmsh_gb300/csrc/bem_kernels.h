@@ -1,0 +1,112 @@
+// Internal interface between the CUDA kernels and the C-ABI layer.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bem_device.cuh"
+
+namespace bem {
+
+// 32-byte node record for the FP32 far-field tiles (bulk-copied to smem).
+struct __align__(16) NodeRec {
+  float xh, xl, yh, yl;  // coordinates as FP32 hi + lo
+  float nx, ny;          // outward normal
+  float cG, cH;          // folded kernel constants times J w
+};
+
+// 32-byte element record: conservative bounding box + squared near limit.
+struct __align__(16) ElemRec {
+  float lox, loy, hix, hiy;
+  float lim2, pad0, pad1, pad2;
+};
+
+struct FarArgs {
+  int nt, n, ne, nn;
+  int64_t ld, ldg;
+  int vec_ok, pair_cap;
+  Physics ph;
+  const float4* rows;
+  const NodeRec* nodes;
+  const ElemRec* elems;
+  const double *px, *py, *nx, *ny, *jac;
+  double ew[BEM_MAXNN];
+  void* H;      // H (or A when fused)
+  void* G;      // G (unused when fused)
+  float* A32;   // FP32 copy of A (mixed precision)
+  const int32_t* bc;
+  const double* bv;
+  double* b;
+  double* rowsum;   // [row * dof + column dof]
+  int* pair_count;
+  int2* pairs;
+  int* status;
+};
+
+struct NearArgs {
+  GeomDev g;
+  Rules R;
+  Physics ph;
+  double near_factor;
+  int64_t ld, ldg;
+  int pair_cap;
+  const int* pair_count;
+  const int2* pairs;
+  void* H;
+  void* G;
+  float* A32;
+  const int32_t* bc;
+  const double* bv;
+  double* b;
+  double* rowsum;
+  double* gdiag;  // on-element G diagonal blocks (fused mode)
+  int mode;       // 0 FP32 H,G; 1 FP64 H,G; 2 FP64 A,b; 3 FP64 + FP32 A,b
+};
+
+struct FinalArgs {
+  int nt, n;
+  int64_t ld;
+  void* H;
+  float* A32;
+  const int32_t* bc;
+  const double* bv;
+  double* b;
+  const double* rowsum;
+  const double* gdiag;
+  int mode;
+};
+
+void launch_near(const NearArgs& na, const FinalArgs& fi, int nc, int nt, int n, cudaStream_t st);
+
+// One assembly request; all pointers are device pointers.
+struct AsmRequest {
+  GeomDev g;
+  Rules R;
+  Physics ph;
+  double near_factor;
+  int prec;    // 0 FP32, 1 FP64, 2 FP64 + FP32 copy of A
+  int fused;   // 1: write A, b (applyBC fused), else H, G
+  void* H;
+  int64_t ld;
+  void* G;
+  int64_t ldg;
+  float* A32;
+  const int32_t* bc;
+  const double* bv;
+  double* b;
+  // workspace
+  float4* rows;
+  NodeRec* nodes;
+  ElemRec* elems;
+  double* rowsum;
+  double* gdiag;
+  int* counters;  // [0] pair count, [1] status
+  int2* pairs;
+  int pair_cap;
+  unsigned long long* absmax;  // scratch: largest |coordinate|
+};
+
+// Launch the whole assembly on `stream` (asynchronous).  Returns 0 or a
+// CUDA error code.
+int launch_assembly(const AsmRequest& q, cudaStream_t stream);
+
+}  // namespace bem

@@ -1,0 +1,137 @@
+/*
+ * bem_gb300.h -- C ABI of the GB300-native dense 2-D BEM collocation path.
+ *
+ * Drop-in for the GPU slot of the Julia package `BEM` (l-s-campos/BEM_gmsh):
+ * `assemble!(dad; method=:gpu)` dispatches to `H_G_gpu`
+ * (src/Core/Assembly_full.jl:112-113), and `solve(dad)` runs `applyBC` +
+ * `bem_linsolve` (src/Core/Solver.jl:24-64, 114-131).  Every entry point
+ * takes plain pointers and sizes, returns an int status (0 = success) and
+ * never throws.  Matrices are column-major (Julia `Matrix` layout) with an
+ * explicit leading dimension, so a `ccall` can write into Julia arrays in
+ * place.  Paths in comments are relative to the reference project root.
+ *
+ * Layout of a problem (what `format2d` builds, src/Core/Input.jl:136-197):
+ *   - ne discontinuous elements of degree p; element e owns the boundary
+ *     collocation nodes e*(p+1) .. e*(p+1)+p (0-based);
+ *   - nt collocation points: the n = ne*(p+1) boundary nodes, then nt-n
+ *     internal points;
+ *   - Laplace: H is nt x nt, G is nt x n; Kelvin: H is 2nt x 2nt, G is
+ *     2nt x 2n, degrees of freedom node-major (2i, 2i+1).
+ */
+#ifndef BEM_GB300_H
+#define BEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define BEM_OK 0
+#define BEM_ERR_INVALID 1       /* bad argument (ArgumentError in the reference) */
+#define BEM_ERR_CUDA 2          /* CUDA runtime error, see bem_last_error() */
+#define BEM_ERR_NOMEM 3         /* device allocation failed */
+#define BEM_ERR_NOT_CONVERGED 4 /* refinement hit its iteration cap */
+#define BEM_ERR_INTERNAL 5      /* a device-side wait timed out */
+#define BEM_ERR_UNSUPPORTED 6   /* size/degree outside the compiled limits */
+
+/* element type of matrix outputs */
+#define BEM_F32 32
+#define BEM_F64 64
+
+/* where the pointers of a call live */
+#define BEM_MEM_HOST 0
+#define BEM_MEM_DEVICE 1
+
+/* solve modes */
+#define BEM_SOLVE_FP64 0  /* FP64 assembly + FP64 LU */
+#define BEM_SOLVE_MIXED 1 /* FP64 A for the residual, TF32 LU, FP64 GMRES-IR */
+
+/*
+ * Boundary mesh of one 2-D problem (the fields `_pack_boundary2d` packs,
+ * src/Laplace/Assembly_GPU.jl:169-228, plus the element CAD nodes
+ * `Element.geo` and lengths `Element.Length`, src/Core/Structures.jl:317-324).
+ * All arrays FP64, host or device memory according to the call's `mem`.
+ */
+typedef struct bem_geom2d {
+  int32_t nt;          /* collocation points (boundary + internal) */
+  int32_t n;           /* boundary nodes = ne * (p + 1) */
+  int32_t ne;          /* elements */
+  int32_t p;           /* field degree: Legendre(p) on Gauss points (1..5) */
+  int32_t ngeo;        /* CAD nodes per element (equispaced), 0 = none */
+  int32_t reserved;
+  const double* px;    /* [nt] collocation x */
+  const double* py;    /* [nt] collocation y */
+  const double* nx;    /* [n] outward normal x */
+  const double* ny;    /* [n] outward normal y */
+  const double* jac;   /* [n] |dx/dxi| at each boundary node (Element.Jacobian) */
+  const double* elen;  /* [ne] element length (Element.Length) */
+  const double* geo_x; /* [ne*ngeo] CAD nodes x (Element.geo), may be NULL if ngeo == 0 */
+  const double* geo_y; /* [ne*ngeo] CAD nodes y */
+  const double* elem_weight; /* [p+1] Gauss weights of the element rule (dad.elem_weight) */
+} bem_geom2d;
+
+typedef struct bem_ctx bem_ctx;
+
+/* Refinement / solve report. */
+typedef struct bem_solve_stats {
+  int32_t status;        /* BEM_OK or BEM_ERR_NOT_CONVERGED */
+  int32_t iterations;    /* GMRES iterations (mixed mode) */
+  double rel_residual;   /* ||b - A x|| / ||b|| in FP64 at exit */
+  double t_assemble_ms;  /* device time of the assembly */
+  double t_factor_ms;    /* device time of the LU */
+  double t_refine_ms;    /* device time of the refinement */
+} bem_solve_stats;
+
+/* Context: one device, one stream, cached device workspace.  Replaces the
+ * per-call KernelAbstractions backend of `_ka_backend`
+ * (src/Laplace/Assembly_GPU.jl:152-167). */
+int bem_ctx_create(int device, bem_ctx** out);
+int bem_ctx_destroy(bem_ctx* ctx);
+/* Run subsequent calls on this cudaStream_t (NULL = the context's own). */
+int bem_ctx_set_stream(bem_ctx* ctx, void* cuda_stream);
+/* Text of the last CUDA error seen by this context. */
+const char* bem_last_error(bem_ctx* ctx);
+const char* bem_status_string(int status);
+
+/*
+ * Dense Laplace H, G.  Replaces `H_G_gpu(dad::BEMdata{<:Laplace}; T, npg,
+ * near, near_factor, device, threaded)` (src/Laplace/Assembly_GPU.jl:120-150)
+ * and returns what `H_G_full_direct` (src/Core/Assembly_full.jl:61-85)
+ * returns: far pairs by nodal lumping, near pairs by the tanp3c map with an
+ * npg-point rule, on-element pairs by interpolated Guiggiani, and the
+ * row-sum diagonal.  dtype BEM_F32: far entries in FP32 math, near and
+ * singular entries in FP64, stored as float; BEM_F64: FP64 throughout.
+ * H: ldh >= nt; G: ldg >= nt.
+ */
+int bem_assemble_laplace2d(bem_ctx* ctx, const bem_geom2d* geom, double k, int npg,
+                           double near_factor, int dtype, int mem, void* H, int64_t ldh,
+                           void* G, int64_t ldg);
+
+/*
+ * Dense Kelvin H, G in 2x2 blocks.  Replaces `H_G_gpu(dad::BEMdata{<:
+ * Elasticity}; ...)` (src/Elasticity/Assembly_GPU.jl:15-51) with the values
+ * of the vectorial `H_G_full_direct` (src/Core/Assembly_full.jl:120-175).
+ * mu: shear modulus; nu_eff: effective Poisson ratio (`effective_nu`,
+ * src/Core/Structures.jl:260-263).  H: ldh >= 2nt; G: ldg >= 2nt.
+ */
+int bem_assemble_kelvin2d(bem_ctx* ctx, const bem_geom2d* geom, double mu, double nu_eff,
+                          int npg, double near_factor, int dtype, int mem, void* H, int64_t ldh,
+                          void* G, int64_t ldg);
+
+/*
+ * Assembly with the boundary-condition column swap fused in: writes the
+ * FP64 system A x = b of `applyBC` (src/Core/Boundary_conditions.jl:54-75
+ * for Laplace, 152-174 for Kelvin) without forming H and G.  kind 0 =
+ * Laplace (prm0 = k), 1 = Kelvin (prm0 = mu, prm1 = nu_eff).  BC/BV have one
+ * entry per boundary DOF (0 = primary field prescribed).
+ */
+int bem_assemble_system2d(bem_ctx* ctx, const bem_geom2d* geom, int kind, double prm0,
+                          double prm1, const int32_t* BC, const double* BV, int npg,
+                          double near_factor, int mem, double* A, int64_t lda, double* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEM_GB300_H */

@@ -1,0 +1,55 @@
+"""CPU-side checks of the C ABI: the library loads and exports every entry
+point declared in include/*.h; argument checks need no GPU."""
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"\b(bem_[a-z0-9_]+)\s*\(", txt):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_declared_symbols():
+    from bem_gmsh_gb300 import _lib, _build
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    L = _lib.load()
+    syms = declared_symbols()
+    assert "bem_assemble_laplace2d" in syms
+    missing = [s for s in sorted(syms) if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_status_strings_and_bad_device():
+    import ctypes
+    from bem_gmsh_gb300 import _lib
+    L = _lib.load()
+    assert L.bem_status_string(0) == b"ok"
+    h = ctypes.c_void_p()
+    # no GPU in this container (or an out-of-range id on a GPU machine): invalid
+    assert L.bem_ctx_create(1 << 20, ctypes.byref(h)) == 1
+
+
+def test_geometry_builders():
+    import numpy as np
+    from bem_gmsh_gb300 import quadrado, star_domain, plate_with_hole
+    d = quadrado(ndiv=20)
+    assert (d.n, d.nt, d.ne) == (152, 513, 76)
+    assert np.allclose(np.linalg.norm(d.normal, axis=1), 1)
+    s = star_domain(2731, p=2, seed=0)
+    assert s.n == 8193 and s.ngeo == 3
+    # outward normals: n . x > 0 on a star-shaped curve around the origin
+    assert np.all(np.sum(s.normal * s.Nodes, axis=1) > 0)
+    pl = plate_with_hole()
+    assert pl.n == (1024 + 342) * 3 and pl.ndof == 2
+    assert int((pl.BC == 0).sum()) == 3

@@ -1,0 +1,130 @@
+"""GPU parity of the assembly against the FP64 oracle, through the C ABI.
+
+Tolerances: FP64 path ||dH||/||H|| < 1e-10 (reference test/laplace.jl:414),
+FP32 path < 1e-6 (test/laplace.jl:454-455)."""
+import numpy as np
+import pytest
+
+from bem_gmsh_gb300 import (quadrado, quadrado_elasticity, star_domain, Elasticity, Laplace,
+                            ana_laplace_linear, attach_analytical, from_cad)
+from bem_gmsh_gb300.api import H_G_gpu, assemble_system
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+TOL32 = 1e-6
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+CASES = [
+    ("quadrado8", lambda: quadrado(ndiv=8, pontointerno=True), 12),
+    ("quadrado10_noint", lambda: quadrado(ndiv=10, pontointerno=False), 12),
+    ("quadrado20", lambda: quadrado(ndiv=20, pontointerno=True), 20),
+    ("quadrado_p2", lambda: quadrado(ndiv=7, ordem=2, pontointerno=True), 16),
+    ("quadrado_p3", lambda: quadrado(ndiv=6, ordem=3, pontointerno=False), 16),
+    ("star_p2", lambda: star_domain(120, p=2, seed=1), 16),
+    ("star_p2_int", lambda: star_domain(90, p=2, seed=2, pontointerno=True), 16),
+    ("star_p1", lambda: star_domain(150, p=1, seed=3), 8),
+]
+
+
+@pytest.mark.parametrize("name,mk,npg", CASES, ids=[c[0] for c in CASES])
+def test_laplace_hg_parity(orc, name, mk, npg):
+    dad = mk()
+    Hr, Gr = orc.assemble(dad, npg=npg, store=False)
+    H, G = H_G_gpu(dad, T=np.float64, npg=npg, store=False)
+    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64, (rel(H, Hr), rel(G, Gr))
+    H32, G32 = H_G_gpu(dad, T=np.float32, npg=npg, store=False)
+    assert rel(H32, Hr) < TOL32 and rel(G32, Gr) < TOL32, (rel(H32, Hr), rel(G32, Gr))
+    assert np.all(np.isfinite(H)) and np.all(np.isfinite(G32))
+
+
+def test_geometry_from_nodes(orc):
+    """ngeo = 0: element geometry from the collocation nodes (no CAD nodes)."""
+    dad = star_domain(80, p=2, seed=4)
+    dad.ngeo = 0
+    dad.geo = np.zeros((dad.ne, 0, 2))
+    Hr, Gr = orc.assemble(dad, npg=16, store=False)
+    H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
+    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64
+
+
+def test_all_near(orc):
+    """near_factor = inf: every pair integrated (no far lumping)."""
+    dad = quadrado(ndiv=6, pontointerno=True)
+    Hr, Gr = orc.assemble(dad, npg=12, near_factor=np.inf, store=False)
+    H, G = H_G_gpu(dad, T=np.float64, npg=12, near_factor=np.inf, store=False)
+    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64
+
+
+@pytest.mark.parametrize("ndiv", [5, 9])
+def test_kelvin_hg_parity(orc, ndiv):
+    dad = quadrado_elasticity(ndiv=ndiv, props=Elasticity(1.0, 0.3, 1.0), pontointerno=True)
+    Hr, Gr = orc.assemble(dad, npg=12, store=False)
+    H, G = H_G_gpu(dad, T=np.float64, npg=12, store=False)
+    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64, (rel(H, Hr), rel(G, Gr))
+    H32, G32 = H_G_gpu(dad, T=np.float32, npg=12, store=False)
+    assert rel(H32, Hr) < TOL32 and rel(G32, Gr) < TOL32, (rel(H32, Hr), rel(G32, Gr))
+
+
+def test_kelvin_curved_plane_stress(orc):
+    pr = Elasticity(E=210e9, nu=0.3, plane_strain=False)
+    dad = star_domain(60, p=2, seed=5, props=pr)
+    dad.BC = np.ones(2 * dad.n, np.int32)
+    dad.BV = np.zeros(2 * dad.n)
+    Hr, Gr = orc.assemble(dad, npg=16, store=False)
+    H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
+    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64, (rel(H, Hr), rel(G, Gr))
+
+
+@pytest.mark.parametrize("kind", ["laplace", "kelvin"])
+def test_fused_system_matches_applybc(orc, kind):
+    if kind == "laplace":
+        dad = star_domain(100, p=2, seed=6, pontointerno=True)
+    else:
+        dad = quadrado_elasticity(ndiv=7, props=Elasticity(1.0, 0.3, 1.0))
+        dad.BC[::3] = 0
+        dad.BV = np.linspace(-1, 1, dad.BV.size)
+    Hr, Gr = orc.assemble(dad, npg=16, store=False)
+    Ar, br = orc.apply_bc(dad, Hr, Gr)
+    A, b = assemble_system(dad, npg=16)
+    assert rel(A, Ar) < TOL64, rel(A, Ar)
+    assert rel(b, br) < TOL64, rel(b, br)
+
+
+def test_device_pointers_and_ld(orc):
+    """BEM_MEM_DEVICE with a padded leading dimension."""
+    import torch
+    dad = star_domain(70, p=2, seed=7, pontointerno=True)
+    Hr, Gr = orc.assemble(dad, npg=16, store=False)
+    ld = dad.nt + 5
+    Hs = torch.zeros((dad.nt, ld), dtype=torch.float64, device="cuda")  # row-major storage of H^T
+    Gs = torch.zeros((dad.n, ld), dtype=torch.float64, device="cuda")
+    H = Hs.t()[: dad.nt]  # column-major view with ld
+    G = Gs.t()[: dad.nt]
+    H_G_gpu(dad, T=np.float64, npg=16, out=(H, G), store=False)
+    assert rel(H.cpu().numpy(), Hr) < TOL64 and rel(G.cpu().numpy(), Gr) < TOL64
+
+
+def test_repeated_calls_reuse_workspace(orc):
+    a = quadrado(ndiv=12, pontointerno=True)
+    b = star_domain(200, p=2, seed=8)
+    for dad in (a, b, a):
+        Hr, Gr = orc.assemble(dad, npg=16, store=False)
+        H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
+        assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64
+
+
+def test_invalid_arguments_raise():
+    from bem_gmsh_gb300._lib import BemError
+    dad = quadrado(ndiv=5)
+    with pytest.raises(ValueError):
+        H_G_gpu(dad, device="cpu")
+    with pytest.raises(ValueError):
+        H_G_gpu(dad, T=np.float16)
+    dad.properties = Laplace(k=-1.0)
+    with pytest.raises(BemError):
+        H_G_gpu(dad)
