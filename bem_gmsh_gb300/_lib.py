@@ -14,6 +14,7 @@ BEM_OK = 0
 BEM_F32, BEM_F64 = 32, 64
 BEM_MEM_HOST, BEM_MEM_DEVICE = 0, 1
 BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
+BEM_OPT_TCGEN05 = 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "refinement did not converge", 5: "device wait timed out", 6: "unsupported"}
@@ -77,6 +78,8 @@ def load(build_if_missing: bool = False):
                         ctypes.c_int),
         "bem_solve_system": ([ctx_p, I64, VP, I64, VP, ctypes.c_int, D, ctypes.c_int, ctypes.c_int, VP,
                               ctypes.POINTER(BemSolveStats)], ctypes.c_int),
+        "bem_ctx_set_option": ([ctx_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+        "bem_selftest": ([ctx_p, ctypes.c_int, ctypes.c_int, PD], ctypes.c_int),
     }
     for name, (args, res) in {**sig, **optional}.items():
         if not hasattr(L, name):
@@ -104,6 +107,16 @@ class Context:
         if rc != BEM_OK:
             msg = self.L.bem_last_error(self.h).decode()
             raise BemError(f"{what}: {STATUS.get(rc, rc)} {msg}".strip())
+
+    def set_option(self, option: int, value: int):
+        self.check(self.L.bem_ctx_set_option(self.h, option, value), "set_option")
+
+    def selftest_lu(self, n: int):
+        """Factor an n x n test matrix with tcgen05 and legacy updates:
+        (max |diff|, max |factor|, ms tcgen05, ms legacy)."""
+        out = (ctypes.c_double * 4)()
+        self.check(self.L.bem_selftest(self.h, 1, n, out), "selftest")
+        return tuple(out)
 
     def set_stream(self, stream_ptr: int):
         self.check(self.L.bem_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")

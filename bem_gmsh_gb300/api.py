@@ -152,3 +152,73 @@ def assemble_system(dad: BEMdata, npg: int = 20, near_factor: float = 1.5, out=N
                                      _ptr(b))
     ctx.check(rc, "assemble_system")
     return A, b
+
+
+def split_sol(dad: BEMdata, x: np.ndarray):
+    """Scatter the solution of A x = b into the fields (`split_sol!`,
+    src/Core/Solver.jl:88-98 for Laplace, 133-146 for elasticity)."""
+    x = np.asarray(x, dtype=np.float64)
+    BC, BV = np.asarray(dad.BC), np.asarray(dad.BV)
+    if dad.ndof == 1:
+        T = x[: dad.nt].copy()
+        q = np.where(BC == 0, T[: dad.n], BV)
+        T[: dad.n] = np.where(BC == 0, BV, T[: dad.n])
+        dad.set_cache(T=T, q=q, x=x)
+        return T
+    nb = 2 * dad.n
+    u = np.where(BC == 0, BV, x[:nb])
+    t = np.where(BC == 0, x[:nb], BV)
+    dad.set_cache(u=u, traction=t, T=u, x=x)
+    return u
+
+
+_MODES = {"mixed": _lib.BEM_SOLVE_MIXED, "fp64": _lib.BEM_SOLVE_FP64}
+
+
+def solve(dad: BEMdata, npg: int = 20, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 200,
+          near_factor: float = 1.5, ctx: _lib.Context | None = None, return_stats: bool = False):
+    """`assemble!` + `solve(dad)` on the GPU: fused assembly of A x = b,
+    then the mixed-precision solve (FP32 tensor-core LU + FP64 GMRES) or the
+    FP64 comparison solve; fills dad.T/dad.q (or dad.u/dad.traction)."""
+    ctx = ctx or _lib.default_context()
+    pr = dad.properties
+    kind = 0 if isinstance(pr, Laplace) else 1
+    p0 = float(pr.k) if kind == 0 else float(pr.mu)
+    p1 = 0.0 if kind == 0 else float(pr.nu_eff)
+    g, keep = geom_struct(dad)
+    BC = np.ascontiguousarray(dad.BC, dtype=np.int32)
+    BV = np.ascontiguousarray(dad.BV, dtype=np.float64)
+    x = np.zeros(pr.ndof * dad.nt)
+    st = _lib.BemSolveStats()
+    rc = ctx.L.bem_solve2d(ctx.h, g, kind, p0, p1, BC.ctypes.data, BV.ctypes.data, int(npg),
+                           float(near_factor), _MODES[mode], float(tol), int(max_iter),
+                           _lib.BEM_MEM_HOST, x.ctypes.data, st)
+    ctx.check(rc, "solve")
+    split_sol(dad, x)
+    stats = dict(iterations=st.iterations, rel_residual=st.rel_residual, t_assemble_ms=st.t_assemble_ms,
+                 t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)
+    dad.set_cache(solve_stats=stats)
+    return (dad.T, stats) if return_stats else dad.T
+
+
+def solve_system(A, b, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 200,
+                 ctx: _lib.Context | None = None):
+    """Dense A x = b (the `bem_linsolve` seam).  A: column-major numpy array
+    or CUDA tensor (FP64); returns (x, stats)."""
+    ctx = ctx or _lib.default_context()
+    dev = _is_torch(A)
+    n = A.shape[0]
+    if dev:
+        import torch
+        x = torch.zeros(n, dtype=torch.float64, device=A.device)
+    else:
+        A = np.asfortranarray(A, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(n)
+    st = _lib.BemSolveStats()
+    rc = ctx.L.bem_solve_system(ctx.h, n, _ptr(A), _ld(A), _ptr(b), _MODES[mode], float(tol),
+                                int(max_iter), _lib.BEM_MEM_DEVICE if dev else _lib.BEM_MEM_HOST,
+                                _ptr(x), st)
+    ctx.check(rc, "solve_system")
+    return x, dict(iterations=st.iterations, rel_residual=st.rel_residual,
+                   t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)

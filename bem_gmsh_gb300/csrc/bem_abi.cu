@@ -127,6 +127,24 @@ void* bem_ctx::get(int slot, size_t bytes) {
   return b.p;
 }
 
+bool bem_ctx::lookahead_ready(int k) {
+  if (!la_stream) {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&la_stream, cudaStreamNonBlocking, hi) != cudaSuccess) {
+      la_stream = nullptr;
+      return false;
+    }
+    if (cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming) != cudaSuccess) return false;
+  }
+  while ((int)events.size() < 2 * k) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+    events.push_back(e);
+  }
+  return true;
+}
+
 int bem_ctx::cuda_fail(cudaError_t e, const char* where) {
   last_error = std::string(where) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? BEM_ERR_NOMEM : BEM_ERR_CUDA;
@@ -158,6 +176,9 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   cudaStreamSynchronize(c->stream);
   for (auto& b : c->slots)
     if (b.p) cudaFree(b.p);
+  for (auto e : c->events) cudaEventDestroy(e);
+  if (c->fork_event) cudaEventDestroy(c->fork_event);
+  if (c->la_stream) cudaStreamDestroy(c->la_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return BEM_OK;

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -14,6 +15,7 @@ struct bem_ctx {
     SLOT_GEOM, SLOT_ROWS, SLOT_NODES, SLOT_ELEMS, SLOT_ROWSUM, SLOT_GDIAG, SLOT_COUNTERS,
     SLOT_PAIRS, SLOT_BC, SLOT_BV, SLOT_OUT0, SLOT_OUT1, SLOT_OUT2, SLOT_OUT3,
     SLOT_LU0, SLOT_LU1, SLOT_LU2, SLOT_LU3, SLOT_LU4, SLOT_LU5, SLOT_LU6, SLOT_LU7,
+    SLOT_TC0, SLOT_TC1, SLOT_TC2, SLOT_TC3, SLOT_TC4, SLOT_TC5, SLOT_TEST0, SLOT_TEST1,
     NSLOT
   };
   struct Buf {
@@ -26,6 +28,14 @@ struct bem_ctx {
   std::string last_error;
   Buf slots[NSLOT];
   int pair_cap_hint = 0;
+  int opt_tcgen05 = 1;  // BEM_OPT_TCGEN05: trailing updates on tcgen05
+
+  // second stream and events of the lookahead LU (created on first use)
+  cudaStream_t la_stream = nullptr;
+  cudaEvent_t fork_event = nullptr;
+  std::vector<cudaEvent_t> events;
+  // Ensures 2*k events and the lookahead stream; false on failure.
+  bool lookahead_ready(int k);
 
   // Grow-only device buffer for `slot` (NULL on allocation failure).
   void* get(int slot, size_t bytes);

@@ -154,17 +154,29 @@ __device__ __forceinline__ void far_eval_f64(const Physics& ph, double rx, doubl
 // --------------------------------------------------------------------------
 // near test (Assembly_full.jl:736-754, Integration.jl:238-312), exact FP64
 // --------------------------------------------------------------------------
+// The near/far decision is discontinuous (integrated vs lumped value), and
+// regular meshes put collocation points exactly on the cut (distance ==
+// 1.5 L).  Every operation below is an explicit IEEE round-to-nearest
+// multiply/add, never a fused multiply-add, so ties resolve exactly as in
+// the reference's IEEE double arithmetic.
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double sq2_(double x, double y) { return add_(mul_(x, x), mul_(y, y)); }
+
 __device__ __forceinline__ double dist_chord(V2 p, V2 a, V2 b) {
-  double abx = b.x - a.x, aby = b.y - a.y;
-  double t = ((p.x - a.x) * abx + (p.y - a.y) * aby) / ((abx * abx + aby * aby) + kEps);
+  double abx = sub_(b.x, a.x), aby = sub_(b.y, a.y);
+  double num = add_(mul_(sub_(p.x, a.x), abx), mul_(sub_(p.y, a.y), aby));
+  double t = __ddiv_rn(num, add_(sq2_(abx, aby), kEps));
   t = fmin(fmax(t, 0.0), 1.0);
-  return vnorm(p.x - (a.x + t * abx), p.y - (a.y + t * aby));
+  double qx = add_(a.x, mul_(t, abx)), qy = add_(a.y, mul_(t, aby));
+  return __dsqrt_rn(sq2_(sub_(p.x, qx), sub_(p.y, qy)));
 }
 
 __device__ __forceinline__ bool near_element(V2 pf, const V2* xg, int n, double L, double factor) {
   if (factor > 1e20) return true;
-  double lim = factor * L;
-  double lim2 = lim * lim;
+  double lim = mul_(factor, L);
+  double lim2 = mul_(lim, lim);
   double dn2 = INFINITY;
   V2 lo = xg[0], hi = xg[0];
   for (int k = 0; k < n; ++k) {
@@ -172,19 +184,18 @@ __device__ __forceinline__ bool near_element(V2 pf, const V2* xg, int n, double 
     lo.y = fmin(lo.y, xg[k].y);
     hi.x = fmax(hi.x, xg[k].x);
     hi.y = fmax(hi.y, xg[k].y);
-    double dx = pf.x - xg[k].x, dy = pf.y - xg[k].y;
-    double d2 = dx * dx + dy * dy;
+    double d2 = sq2_(sub_(pf.x, xg[k].x), sub_(pf.y, xg[k].y));
     if (d2 < dn2) dn2 = d2;
   }
   if (dn2 < lim2) return true;
   double d2 = 0.0;
-  if (pf.x < lo.x) { double t = lo.x - pf.x; d2 += t * t; }
-  else if (pf.x > hi.x) { double t = pf.x - hi.x; d2 += t * t; }
-  if (pf.y < lo.y) { double t = lo.y - pf.y; d2 += t * t; }
-  else if (pf.y > hi.y) { double t = pf.y - hi.y; d2 += t * t; }
-  if (sqrt(d2) >= lim) return false;
+  if (pf.x < lo.x) { double t = sub_(lo.x, pf.x); d2 = add_(d2, mul_(t, t)); }
+  else if (pf.x > hi.x) { double t = sub_(pf.x, hi.x); d2 = add_(d2, mul_(t, t)); }
+  if (pf.y < lo.y) { double t = sub_(lo.y, pf.y); d2 = add_(d2, mul_(t, t)); }
+  else if (pf.y > hi.y) { double t = sub_(pf.y, hi.y); d2 = add_(d2, mul_(t, t)); }
+  if (__dsqrt_rn(d2) >= lim) return false;
   double d = INFINITY;
-  if (n == 1) d = vnorm(pf.x - xg[0].x, pf.y - xg[0].y);
+  if (n == 1) d = __dsqrt_rn(sq2_(sub_(pf.x, xg[0].x), sub_(pf.y, xg[0].y)));
   for (int k = 0; k + 1 < n; ++k) d = fmin(d, dist_chord(pf, xg[k], xg[k + 1]));
   return d < lim;
 }

@@ -1,0 +1,66 @@
+// Internal interface of the dense solve kernels (lu.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define LU_NB 128  // LU block size (rows/columns of a diagonal block)
+
+namespace bem {
+
+// cs[j] = 1 / max_i |A[i, j]|; A32 = A * diag(cs) in FP32, identity padding
+// up to Npad (a multiple of LU_NB).
+void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, float* A32,
+                int64_t ld32, cudaStream_t st);
+// In-place blocked LU without pivoting of the Npad x Npad FP32 matrix.
+// Dinv receives, per diagonal block, the inverses of its unit-lower and
+// upper triangles (2 x LU_NB^2 floats per block).  info: first block with a
+// vanishing pivot (1-based), untouched otherwise.  x3: 3xTF32 updates.
+struct TcPlan;
+int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
+              const TcPlan* tc = nullptr, int* err = nullptr);
+// out <- U^{-1} L^{-1} r on padded FP32 vectors.  tmp: Npad floats (the
+// forward result), flags: 2 Npad/LU_NB ints, err: timeout flag.  r may be
+// clobbered.  Returns 0 or a CUDA error code.
+int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
+                 float* out, int* flags, int* err, cudaStream_t st);
+
+void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
+                cudaStream_t st);
+void gemv64(const double* A, int64_t lda, int N, const double* x, double* y, cudaStream_t st);
+void dots64(const double* V, int64_t ldv, int N, int m, const double* w, double* h, cudaStream_t st);
+void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, double* w, cudaStream_t st);
+void add_zy64(const double* Z, int64_t ldz, int N, int m, const double* y, double* x, cudaStream_t st);
+void scale_copy64(const double* w, double s, double* v, int N, cudaStream_t st);
+void to_f32(const double* v, int N, int Npad, float* o, cudaStream_t st);
+void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStream_t st);
+
+// C (M x N) = beta C + alpha A (M x 128) B (128 x N); M, N multiples of 128.
+void gemm_tile128(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                  int M, int N, float alpha, float beta, int x3, cudaStream_t st);
+
+// tcgen05 trailing update (gemm_tc.cu).  The plan holds the TMA maps of the
+// transposed L panel, its lo part, the matrix (U panel) and the U lo part.
+struct TcPlan {
+  float* A = nullptr;
+  int64_t ld = 0;
+  int Npad = 0;
+  float* Lt = nullptr;    // Npad x 128, K-major
+  float* Ltlo = nullptr;  // Npad x 128
+  float* Ulo = nullptr;   // 128 x Npad (K-major per column)
+  alignas(64) unsigned char mA[128];
+  alignas(64) unsigned char mAlo[128];
+  alignas(64) unsigned char mB[128];
+  alignas(64) unsigned char mBlo[128];
+  bool ok = false;
+};
+bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, float* Ulo);
+// Lt, Ltlo, Ulo of step k (from the factored panels)
+void tc_split(const TcPlan& p, int k, cudaStream_t st);
+// part of step k's trailing update: rows [ro, ro+M), columns [co, co+N) of
+// the trailing matrix  A22 -= L21 U12
+int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st);
+int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
+                        cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
+                        const TcPlan* tc, int* err);
+
+}  // namespace bem

@@ -1,0 +1,378 @@
+// Trailing-update GEMM of the blocked LU on the 5th-generation tensor cores
+// (sm_103a): C (M x N) = beta C + alpha A (M x 128) B (128 x N) in FP32 with
+// the 3xTF32 split  A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi.
+//
+// One CTA computes a 128 x 256 tile:
+//   warp 0, one lane : TMA producer.  Per 32-wide k chunk it loads A_hi, A_lo
+//                      (128 x 32) and B_hi, B_lo (256 x 32), K-major with the
+//                      128-byte swizzle, into a 2-stage ring.
+//   warp 1, one lane : MMA issuer.  tcgen05.mma.kind::tf32, M=128, N=256,
+//                      K=8 per instruction, accumulator in TMEM (256 columns).
+//                      tcgen05.commit frees a stage / signals the epilogue.
+//   warps 0-7        : epilogue.  tcgen05.ld 32x32b: thread = row, 32
+//                      columns per load, two warps per TMEM lane quadrant
+//                      (column halves); C read/modify/write in batches of
+//                      32 loads, coalesced per column (a warp covers 32
+//                      consecutive rows).
+// The tensor core reads the top 19 bits of an FP32 operand (TF32), so the
+// FP32 matrix itself is the "hi" operand; the "lo" operands x - tf32(x) are
+// precomputed by k_split_lo.  Every mbarrier wait is bounded: on timeout
+// the CTA records an error, leaves the tile unwritten and frees its TMEM.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "bem_lu.h"
+
+namespace bem {
+
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int BK = 32;  // one 128-byte swizzle atom of FP32
+constexpr int STAGES = 2;
+constexpr int A_BYTES = BM * BK * 4;  // 16 KB
+constexpr int B_BYTES = BN * BK * 4;  // 32 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t TMEM_COLS = 256;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+// bounded wait for the given phase parity; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 20); ++it) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), leading offset unused for this layout (1).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, M=128, N=256
+constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          dtmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
+        "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
+        "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TcArgs {
+  float* C;
+  int64_t ldc;
+  int M, N;       // valid extent of C (M multiple of 128)
+  int ay0;        // row (m) coordinate of the first A row in the A maps
+  int bx0, by0;   // B maps: k coordinate and n coordinate of B(0, 0)
+  int blx0, bly0; // B lo map: same for the lo copy
+  float alpha, beta;
+  int* err;
+};
+
+__global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUtensorMap mA,
+                                                    const __grid_constant__ CUtensorMap mAlo,
+                                                    const __grid_constant__ CUtensorMap mB,
+                                                    const __grid_constant__ CUtensorMap mBlo,
+                                                    TcArgs a) {
+  extern __shared__ __align__(1024) uint8_t dsm[];
+  // 1024-byte aligned tile area
+  const uint32_t base_u = smem_u32(dsm);
+  const uint32_t tiles = (base_u + 1023u) & ~1023u;
+  uint8_t* misc = dsm + (tiles - base_u) + STAGES * STAGE_BYTES;
+  uint64_t* bars = (uint64_t*)misc;  // full[2], empty[2], done
+  uint32_t* s_tmem = (uint32_t*)(misc + 64);
+  int* s_fail = (int*)(misc + 72);
+  const uint32_t full0 = smem_u32(&bars[0]);
+  const uint32_t empty0 = smem_u32(&bars[2]);
+  const uint32_t done = smem_u32(&bars[4]);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+
+  if (threadIdx.x == 0) {
+    mbar_init(full0, 1);
+    mbar_init(full0 + 8, 1);
+    mbar_init(empty0, 1);
+    mbar_init(empty0 + 8, 1);
+    mbar_init(done, 1);
+    *s_fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *s_tmem;
+  constexpr int NCH = LU_NB / BK;  // 4 k chunks
+
+  if (warp == 0 && lane == 0) {
+    // producer
+    for (int c = 0; c < NCH; ++c) {
+      const int s = c % STAGES;
+      if (c >= STAGES) {
+        if (!mbar_wait(empty0 + 8 * s, ((c / STAGES) - 1) & 1)) { atomicExch(s_fail, 1); break; }
+      }
+      const uint32_t st = tiles + s * STAGE_BYTES;
+      mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
+      tma_load_2d(st, &mA, c * BK, a.ay0 + m0, full0 + 8 * s);
+      tma_load_2d(st + A_BYTES, &mAlo, c * BK, a.ay0 + m0, full0 + 8 * s);
+      tma_load_2d(st + 2 * A_BYTES, &mB, a.bx0 + c * BK, a.by0 + n0, full0 + 8 * s);
+      tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBlo, a.blx0 + c * BK, a.bly0 + n0, full0 + 8 * s);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    bool ok = true;
+    for (int c = 0; c < NCH && ok; ++c) {
+      const int s = c % STAGES;
+      if (!mbar_wait(full0 + 8 * s, (c / STAGES) & 1)) { atomicExch(s_fail, 1); ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = tiles + s * STAGE_BYTES;
+      const uint64_t dah = sdesc(st), dal = sdesc(st + A_BYTES);
+      const uint64_t dbh = sdesc(st + 2 * A_BYTES), dbl = sdesc(st + 2 * A_BYTES + B_BYTES);
+#pragma unroll
+      for (int ks = 0; ks < BK / 8; ++ks) {
+        const uint64_t off = (uint64_t)((ks * 32) >> 4);  // 32 bytes per k step
+        const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+        mma_tf32(tmem, dal + off, dbh + off, acc0);
+        mma_tf32(tmem, dah + off, dbl + off, 1u);
+        mma_tf32(tmem, dah + off, dbh + off, 1u);
+      }
+      mma_commit(empty0 + 8 * s);
+    }
+    mma_commit(done);
+  }
+  __syncwarp();
+  // epilogue: all four warps; the go/no-go decision is block-uniform
+  const bool got = mbar_wait(done, 0);
+  const int all_ok = __syncthreads_and(got ? 1 : 0);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int fail = *((volatile int*)s_fail);
+  if (all_ok && !fail) {
+    // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and the
+    // column half w / 4; 32 C values are loaded before any is stored
+    const int quad = warp & 3, half = warp >> 2;
+    const int row = m0 + quad * 32 + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
+    float* Crow = a.C + row;
+    for (int cb = half * (BN / 2); cb < (half + 1) * (BN / 2); cb += 32) {
+      uint32_t v[32];
+      tmem_ld32(lane_addr + cb, v);
+      if (row < a.M) {
+        float cv[32];
+        if (a.beta != 0.f) {
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const int col = n0 + cb + q;
+            cv[q] = (col < a.N) ? __ldcs(Crow + (size_t)col * a.ldc) : 0.f;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int col = n0 + cb + q;
+          if (col < a.N) {
+            const float accv = __uint_as_float(v[q]);
+            const float r = (a.beta == 0.f) ? a.alpha * accv : a.beta * cv[q] + a.alpha * accv;
+            __stcs(Crow + (size_t)col * a.ldc, r);
+          }
+        }
+      }
+    }
+  } else {
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+    // let any MMA still in flight finish before the accumulator is freed
+    if (!all_ok) mbar_wait(done, 0);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------
+// lo parts and the transposed L panel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float tf32_trunc(float x) {
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+
+// Lt[m][k] = L21[m][k] (K-major copy), Ltlo = Lt - tf32(Lt);
+// U12lo[k][n] = U12 - tf32(U12)  (same K-major layout as U12 in the matrix)
+__global__ void k_split_lo(const float* __restrict__ A, int64_t ld, int kk, int rem,
+                           float* __restrict__ Lt, float* __restrict__ Ltlo, float* __restrict__ Ulo) {
+  __shared__ float tile[32][33];
+  // L21: rows kk+128 .., columns kk..kk+127 -> Lt (rem x 128)
+  const int mt = blockIdx.x * 32, kt = blockIdx.y * 32;
+  if (mt < rem) {
+    const float* L = A + (size_t)(kk + LU_NB) + (size_t)kk * ld;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+      tile[i][threadIdx.x] = L[(size_t)(mt + threadIdx.x) + (size_t)(kt + i) * ld];
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const float v = tile[threadIdx.x][i];
+      const size_t o = (size_t)(mt + i) * LU_NB + kt + threadIdx.x;
+      Lt[o] = v;
+      Ltlo[o] = v - tf32_trunc(v);
+    }
+    // U12: rows kk..kk+127, columns kk+128+mt.. (reuse the m index as n)
+    const float* U = A + (size_t)kk + (size_t)(kk + LU_NB) * ld;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const size_t n = (size_t)(mt + i);
+      const float v = U[(size_t)(kt + threadIdx.x) + n * ld];
+      Ulo[(size_t)(kt + threadIdx.x) + n * LU_NB] = v - tf32_trunc(v);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                CUtensorMapFloatOOBfill);
+
+static EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiled)p;
+  }
+  return fn;
+}
+
+// 2-D FP32 map: inner dimension `inner` (contiguous), outer `outer`, row
+// pitch `pitch` elements, box 32 x box_outer, 128-byte swizzle.
+static bool make_map(CUtensorMap* m, const float* base, uint64_t inner, uint64_t outer, uint64_t pitch,
+                     uint32_t box_outer) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {pitch * 4};
+  cuuint32_t box[2] = {32, box_outer};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, float* Ulo) {
+  p.A = A;
+  p.ld = ld;
+  p.Npad = Npad;
+  p.Lt = Lt;
+  p.Ltlo = Ltlo;
+  p.Ulo = Ulo;
+  p.ok = make_map((CUtensorMap*)p.mA, Lt, LU_NB, (uint64_t)Npad, LU_NB, tc::BM) &&
+         make_map((CUtensorMap*)p.mAlo, Ltlo, LU_NB, (uint64_t)Npad, LU_NB, tc::BM) &&
+         make_map((CUtensorMap*)p.mB, A, (uint64_t)Npad, (uint64_t)Npad, (uint64_t)ld, tc::BN) &&
+         make_map((CUtensorMap*)p.mBlo, Ulo, LU_NB, (uint64_t)Npad, LU_NB, tc::BN);
+  if (p.ok) {
+    cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+  }
+  return p.ok;
+}
+
+void tc_split(const TcPlan& p, int k, cudaStream_t st) {
+  const int kk = k * LU_NB;
+  const int rem = p.Npad - kk - LU_NB;
+  if (rem <= 0) return;
+  dim3 sg(rem / 32, LU_NB / 32);
+  k_split_lo<<<sg, dim3(32, 8), 0, st>>>(p.A, p.ld, kk, rem, p.Lt, p.Ltlo, p.Ulo);
+}
+
+int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return 0;
+  const int kk = k * LU_NB;
+  tc::TcArgs a{};
+  a.C = p.A + (size_t)(kk + LU_NB + ro) + (size_t)(kk + LU_NB + co) * p.ld;
+  a.ldc = p.ld;
+  a.M = M;
+  a.N = N;
+  a.ay0 = ro;
+  a.bx0 = kk;
+  a.by0 = kk + LU_NB + co;
+  a.blx0 = 0;
+  a.bly0 = co;
+  a.alpha = -1.f;
+  a.beta = 1.f;
+  a.err = err;
+  dim3 grid(M / tc::BM, (N + tc::BN - 1) / tc::BN);
+  tc::k_gemm_tc<<<grid, 256, tc::SMEM_BYTES, st>>>(*(const CUtensorMap*)p.mA, *(const CUtensorMap*)p.mAlo,
+                                                    *(const CUtensorMap*)p.mB, *(const CUtensorMap*)p.mBlo,
+                                                    a);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace bem

@@ -1,0 +1,870 @@
+// Dense solve kernels: column equilibration, blocked LU without pivoting
+// (FP32 storage, TF32 tensor-core updates), triangular solves with the
+// factors, and the FP64 vector kernels of the refinement loop.
+//
+// The reference solves A x = b with LinearSolve.jl's dense LU
+// (src/Core/LinearSolveUtils.jl:44-49, LAPACK getrf/getrs with partial
+// pivoting).  Here A is first equilibrated by columns; BEM collocation
+// systems equilibrated this way factor stably without row exchanges
+// (growth factors of order 1-10 on the Laplace and Kelvin test systems), so
+// the factorization needs no pivot search across the panel, which is the
+// latency bottleneck of partial pivoting on a GPU.  The FP32 factors only
+// precondition an FP64 GMRES whose residual uses the FP64 matrix, so the
+// final solution has FP64 accuracy.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "bem_lu.h"
+
+namespace bem {
+
+// ---------------------------------------------------------------------------
+// equilibration + FP32 copy with identity padding
+// ---------------------------------------------------------------------------
+__global__ void k_colscale(const double* __restrict__ A, int64_t lda, int N, double* __restrict__ cs) {
+  const int j = blockIdx.x;
+  if (j >= N) return;
+  const double* col = A + (size_t)j * lda;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) m = fmax(m, fabs(col[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double s[32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, s[w]);
+    cs[j] = (r > 0.0 && r < INFINITY) ? 1.0 / r : 1.0;
+  }
+}
+
+// A32[i, j] = A[i, j] * cs[j] for i, j < N; identity on the padding.
+__global__ void k_scale_convert(const double* __restrict__ A, int64_t lda, int N, int Npad,
+                                const double* __restrict__ cs, float* __restrict__ A32, int64_t ld32) {
+  const int j = blockIdx.y;
+  const double s = j < N ? cs[j] : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Npad; i += gridDim.x * blockDim.x) {
+    float v;
+    if (i < N && j < N) v = (float)(A[i + (size_t)j * lda] * s);
+    else v = (i == j) ? 1.f : 0.f;
+    A32[i + (size_t)j * ld32] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// diagonal block: unblocked LU of a 128 x 128 block in shared memory, then
+// the inverses of its unit-lower and upper triangles.
+// ---------------------------------------------------------------------------
+constexpr int DLD = LU_NB + 1;
+
+// Gauss-Jordan form: the forward elimination applied to [A | I] leaves U in
+// A and L^{-1} in the identity part; the backward sweep on [U | I] builds
+// U^{-1} one row at a time, pushing each finished row into the rows above.
+// Every step is one block-wide barrier pair; all work inside a step is
+// spread over the 512 threads.
+__global__ void __launch_bounds__(512) k_diag_factor(float* __restrict__ A, int64_t ld, int k,
+                                                     float* __restrict__ Dinv, int* __restrict__ info) {
+  extern __shared__ float sm[];
+  float* s = sm;                    // [col][row], ld DLD: A -> L\U
+  float* li = sm + LU_NB * DLD;     // Linv, [col][row]
+  float* ui = li + LU_NB * DLD;     // Uinv, [col][row]
+  __shared__ float lcol[LU_NB];
+  __shared__ int bad;
+  const int t = threadIdx.x;
+  const size_t off = (size_t)k * LU_NB;
+  float* Ab = A + off + off * ld;
+  if (t == 0) bad = 0;
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    s[c * DLD + r] = Ab[r + (size_t)c * ld];
+    li[c * DLD + r] = (r == c) ? 1.f : 0.f;
+    ui[c * DLD + r] = 0.f;
+  }
+  __syncthreads();
+  // forward elimination on [A | I]
+  for (int j = 0; j < LU_NB; ++j) {
+    const float piv = s[j * DLD + j];
+    if (t == 0 && !(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
+    const float inv = 1.f / piv;
+    for (int r = j + 1 + t; r < LU_NB; r += blockDim.x) {
+      float l = s[j * DLD + r] * inv;
+      lcol[r] = l;
+      s[j * DLD + r] = l;  // multiplier stored as L
+    }
+    __syncthreads();
+    // columns j+1..127 of A and columns 0..j of Linv: thread owns column
+    // (t & 127) and every 4th row; conflict-free ([col][row], ld 129)
+    {
+      const int cc = t & (LU_NB - 1);
+      const int r0 = j + 1 + (t >> 7);
+      if (cc > j) {
+        const float u = s[cc * DLD + j];
+        for (int r = r0; r < LU_NB; r += 4) s[cc * DLD + r] -= lcol[r] * u;
+      } else {
+        const float u = li[cc * DLD + j];
+        for (int r = r0; r < LU_NB; r += 4) li[cc * DLD + r] -= lcol[r] * u;
+      }
+    }
+    __syncthreads();
+  }
+  // backward sweep: U X = I, rows from the bottom
+  for (int j = LU_NB - 1; j >= 0; --j) {
+    const float inv = 1.f / s[j * DLD + j];
+    // finish row j: X[j][c] = (I[j][c] - pushed terms) / u_jj for c >= j
+    for (int c = j + t; c < LU_NB; c += blockDim.x) {
+      float v = ((c == j) ? 1.f : 0.f) + ui[c * DLD + j];
+      ui[c * DLD + j] = v * inv;
+    }
+    __syncthreads();
+    // push into rows r < j: R[r][c] -= u_rj X[j][c], c >= j (accumulated in ui with sign)
+    {
+      const int c = t & (LU_NB - 1);
+      if (c >= j) {
+        const float xj = ui[c * DLD + j];
+        for (int r = t >> 7; r < j; r += 4) ui[c * DLD + r] -= s[j * DLD + r] * xj;
+      }
+    }
+    __syncthreads();
+  }
+  if (t == 0 && bad) atomicExch(info, k + 1);
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    Ab[r + (size_t)c * ld] = s[c * DLD + r];
+  }
+  float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  float* Ui = Li + LU_NB * LU_NB;
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    Li[r + c * LU_NB] = li[c * DLD + r];
+    Ui[r + c * LU_NB] = ui[c * DLD + r];
+  }
+}
+
+// Register-blocked version of the same Gauss-Jordan factorization.  Warp w
+// (0..15) owns rows w, w+16, ..., w+112 and lane l owns columns l, l+32,
+// l+64, l+96, so every thread holds an 8 x 4 tile of [A | I] in registers.
+// Step j publishes row j (one warp) and column j (one lane per warp) to
+// shared memory, double-buffered by step parity, then one barrier; the
+// row loads are conflict-free and the column loads are broadcasts.
+// Forward elimination leaves L\U in `a` and L^{-1} in `b`; the backward sweep
+// then turns a fresh identity in `b` into U^{-1}.
+__global__ void __launch_bounds__(512) k_diag_factor_rb(float* __restrict__ A, int64_t ld, int k,
+                                                        float* __restrict__ Dinv, int* __restrict__ info) {
+  extern __shared__ float stage[];  // LU_NB * DLD
+  __shared__ float prow[2][LU_NB], pcol[2][LU_NB], pb[2][LU_NB];
+  __shared__ int bad;
+  const int t = threadIdx.x;
+  const int lane = t & 31, w = t >> 5;
+  const size_t off = (size_t)k * LU_NB;
+  float* Ab = A + off + off * ld;
+  if (t == 0) bad = 0;
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    stage[c * DLD + r] = Ab[r + (size_t)c * ld];
+  }
+  __syncthreads();
+  float a[8][4], b[8][4];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = w + 16 * i, c = lane + 32 * q;
+      a[i][q] = stage[c * DLD + r];
+      b[i][q] = (r == c) ? 1.f : 0.f;
+    }
+  // forward elimination on [A | I]
+  for (int j = 0; j < LU_NB; ++j) {
+    const int p = j & 1;
+    if (w == (j & 15)) {
+      const int ij = j >> 4;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i == ij) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            prow[p][lane + 32 * q] = a[i][q];
+            pb[p][lane + 32 * q] = b[i][q];
+          }
+        }
+    }
+    if (lane == (j & 31)) {
+      const int qj = j >> 5;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == qj) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) pcol[p][w + 16 * i] = a[i][q];
+        }
+    }
+    __syncthreads();
+    const float piv = pcol[p][j];
+    if (t == 0 && !(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
+    const float inv = 1.f / piv;
+    // branch-free update: multipliers of inactive rows are 0, the row-j
+    // values feed the U part for columns > j and the L^{-1} part otherwise
+    float fa[4], fb[4], l[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool right = (lane + 32 * q) > j;
+      const float rv = prow[p][lane + 32 * q], bv = pb[p][lane + 32 * q];
+      fa[q] = right ? rv : 0.f;
+      fb[q] = right ? 0.f : bv;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) l[i] = (w + 16 * i > j) ? pcol[p][w + 16 * i] * inv : 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[i][q] -= l[i] * fa[q];
+        b[i][q] -= l[i] * fb[q];
+      }
+    if (lane == (j & 31)) {  // store the multipliers as column j of L
+      const int qj = j >> 5;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == qj) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i)
+            if (w + 16 * i > j) a[i][q] = l[i];
+        }
+    }
+  }
+  __syncthreads();
+  float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  float* Ui = Li + LU_NB * LU_NB;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) stage[(lane + 32 * q) * DLD + w + 16 * i] = a[i][q];
+  __syncthreads();
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    Ab[r + (size_t)c * ld] = stage[c * DLD + r];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = w + 16 * i, c = lane + 32 * q;
+      stage[c * DLD + r] = b[i][q];
+      b[i][q] = (r == c) ? 1.f : 0.f;
+    }
+  __syncthreads();
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    Li[r + c * LU_NB] = stage[c * DLD + r];
+  }
+  // backward sweep: U X = I from the bottom row up.  Step j publishes the
+  // accumulated row j of X (before scaling) and column j of U.
+  for (int j = LU_NB - 1; j >= 0; --j) {
+    const int p = j & 1;
+    if (w == (j & 15)) {
+      const int ij = j >> 4;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i == ij) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) pb[p][lane + 32 * q] = b[i][q];
+        }
+    }
+    if (lane == (j & 31)) {
+      const int qj = j >> 5;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == qj) {
+#pragma unroll
+          for (int i = 0; i < 8; ++i) pcol[p][w + 16 * i] = a[i][q];
+        }
+    }
+    __syncthreads();
+    const float inv = 1.f / pcol[p][j];
+    float xv[4], u[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) xv[q] = (lane + 32 * q >= j) ? pb[p][lane + 32 * q] * inv : 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) u[i] = (w + 16 * i < j) ? pcol[p][w + 16 * i] : 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) b[i][q] -= u[i] * xv[q];
+    if (w == (j & 15)) {  // finished row j of U^{-1}
+      const int ij = j >> 4;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i == ij) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q >= j) b[i][q] = xv[q];
+        }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) stage[(lane + 32 * q) * DLD + w + 16 * i] = b[i][q];
+  __syncthreads();
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int r = idx & (LU_NB - 1), c = idx >> 7;
+    Ui[r + c * LU_NB] = stage[c * DLD + r];
+  }
+  if (t == 0 && bad) atomicExch(info, k + 1);
+}
+
+// ---------------------------------------------------------------------------
+// 128 x 128 x 128 tile GEMM on the legacy tensor-core path (mma.sync TF32),
+// optionally with the 3xTF32 split (hi*hi + hi*lo + lo*hi) for FP32
+// accuracy.  C = beta * C + alpha * A * B, column-major.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int GK = 32;          // k chunk
+constexpr int ALD = 128 + 4;    // As[k][m]
+constexpr int BLD = GK + 4;     // Bs[n][k]
+
+template <bool X3>
+__global__ void __launch_bounds__(256) k_gemm_mma(const float* A, int64_t lda,
+                                                  const float* B, int64_t ldb,
+                                                  float* C, int64_t ldc, float alpha, float beta) {
+  extern __shared__ __align__(16) float gsm[];
+  float* As = gsm;                       // 2 stages of [GK][ALD]
+  float* Bs = gsm + 2 * GK * ALD;        // 2 stages of [128][BLD]
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, warp tile 64 x 32
+  const int g = lane >> 2, tg = lane & 3;
+  const size_t m0 = (size_t)blockIdx.x * 128, n0 = (size_t)blockIdx.y * 128;
+  const float* Ab = A + m0;
+  const float* Bb = B + n0 * ldb;
+
+  auto load = [&](int stage, int kc) {
+    float* as = As + stage * GK * ALD;
+    float* bs = Bs + stage * 128 * BLD;
+    for (int s = t; s < GK * 32; s += 256) {  // A: 32 k-columns x 32 segments of 4 m
+      int kk = s >> 5, seg = s & 31;
+      cp_async16(as + kk * ALD + seg * 4, Ab + (size_t)(kc + kk) * lda + seg * 4);
+    }
+    for (int s = t; s < 128 * 8; s += 256) {  // B: 128 n-columns x 8 segments of 4 k
+      int nn = s >> 3, seg = s & 7;
+      cp_async16(bs + nn * BLD + seg * 4, Bb + (size_t)nn * ldb + kc + seg * 4);
+    }
+    cp_async_commit();
+  };
+
+  float acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+
+  load(0, 0);
+  constexpr int NCH = LU_NB / GK;
+  for (int ch = 0; ch < NCH; ++ch) {
+    if (ch + 1 < NCH) {
+      load((ch + 1) & 1, (ch + 1) * GK);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float* as = As + (ch & 1) * GK * ALD;
+    const float* bs = Bs + (ch & 1) * 128 * BLD;
+#pragma unroll
+    for (int k8 = 0; k8 < GK; k8 += 8) {
+      uint32_t ah[4][4], al[4][4], bh[4][2], bl[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int mr = wm * 64 + i * 16 + g;
+        float v[4] = {as[(k8 + tg) * ALD + mr], as[(k8 + tg) * ALD + mr + 8],
+                      as[(k8 + tg + 4) * ALD + mr], as[(k8 + tg + 4) * ALD + mr + 8]};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          ah[i][q] = tf32_rna(v[q]);
+          if (X3) al[i][q] = tf32_rna(v[q] - __uint_as_float(ah[i][q]));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int nc = wn * 32 + j * 8 + g;
+        float v[2] = {bs[nc * BLD + k8 + tg], bs[nc * BLD + k8 + tg + 4]};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          bh[j][q] = tf32_rna(v[q]);
+          if (X3) bl[j][q] = tf32_rna(v[q] - __uint_as_float(bh[j][q]));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (X3) {
+            mma_tf32(acc[i][j], al[i], bh[j]);
+            mma_tf32(acc[i][j], ah[i], bl[j]);
+          }
+          mma_tf32(acc[i][j], ah[i], bh[j]);
+        }
+    }
+    __syncthreads();
+  }
+  // epilogue
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const size_t r0 = m0 + wm * 64 + i * 16 + g;
+      const size_t c0 = n0 + wn * 32 + j * 8 + 2 * tg;
+      float* p00 = C + r0 + c0 * ldc;
+      float* p01 = C + r0 + (c0 + 1) * ldc;
+      float* p10 = p00 + 8;
+      float* p11 = p01 + 8;
+      if (beta == 0.f) {
+        *p00 = alpha * acc[i][j][0];
+        *p01 = alpha * acc[i][j][1];
+        *p10 = alpha * acc[i][j][2];
+        *p11 = alpha * acc[i][j][3];
+      } else {
+        *p00 = beta * *p00 + alpha * acc[i][j][0];
+        *p01 = beta * *p01 + alpha * acc[i][j][1];
+        *p10 = beta * *p10 + alpha * acc[i][j][2];
+        *p11 = beta * *p11 + alpha * acc[i][j][3];
+      }
+    }
+}
+
+size_t gemm_mma_smem() { return sizeof(float) * (2 * GK * ALD + 2 * 128 * BLD); }
+
+// C (M x N, multiples of 128) = beta C + alpha A (M x 128) B (128 x N)
+void gemm_tile128(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
+                  int M, int N, float alpha, float beta, int x3, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid(M / 128, N / 128);
+  const size_t sm = gemm_mma_smem();
+  if (x3)
+    k_gemm_mma<true><<<grid, 256, sm, st>>>(A, lda, B, ldb, C, ldc, alpha, beta);
+  else
+    k_gemm_mma<false><<<grid, 256, sm, st>>>(A, lda, B, ldb, C, ldc, alpha, beta);
+}
+
+// ---------------------------------------------------------------------------
+// triangular solves with the blocked factors (FP32), one block row per step
+// ---------------------------------------------------------------------------
+// y[kb] = Dk * r[kb], Dk = 128 x 128 inverse block; r, y FP32 (may alias)
+__global__ void k_blk_apply(const float* __restrict__ D, const float* r, float* y) {
+  __shared__ float rs[LU_NB];
+  const int t = threadIdx.x;
+  rs[t] = r[t];
+  __syncthreads();
+  float acc = 0.f;
+#pragma unroll 8
+  for (int q = 0; q < LU_NB; ++q) acc += D[t + q * LU_NB] * rs[q];
+  y[t] = acc;
+}
+
+// r[rows] -= P[rows, 0:128] * y, P column-major with ld
+__global__ void k_panel_gemv(const float* __restrict__ P, int64_t ld, int rows,
+                             const float* __restrict__ y, float* r) {
+  __shared__ float ys[LU_NB];
+  if (threadIdx.x < LU_NB) ys[threadIdx.x] = y[threadIdx.x];
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+    float acc = 0.f;
+#pragma unroll 8
+    for (int q = 0; q < LU_NB; ++q) acc += P[i + (size_t)q * ld] * ys[q];
+    r[i] -= acc;
+  }
+}
+
+// r[0:rows] -= P[0:rows, :] * y for an upper-triangular sweep (P = column block)
+// same kernel as k_panel_gemv; kept separate for clarity of the launch sites.
+
+// ---------------------------------------------------------------------------
+// Wavefront triangular solve: one CTA per block row, one launch per sweep.
+// CTA q of the forward sweep computes y_b (b = q) = Linv_b (r_b - sum_{j<b}
+// L_bj y_j); the backward sweep runs b = K-1-q downwards with U and Uinv_b.
+// A CTA waits only for lower-numbered CTAs (flags set with release
+// semantics after their block is written); the waits are bounded and a
+// timeout is reported through `err` instead of hanging.  The launch is
+// cooperative so that all CTAs are resident.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <bool UPPER>
+__global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, int64_t ld, int K,
+                                                   const float* __restrict__ Dinv, const float* r,
+                                                   float* y, int* flags, int epoch, int* err) {
+  extern __shared__ float Ds[];  // the block's inverse, [col][row], LU_NB * (LU_NB + 1)
+  __shared__ float ys[LU_NB];
+  __shared__ float part[2][LU_NB];
+  __shared__ int ok;
+  const int t = threadIdx.x, row = t & (LU_NB - 1), half = t >> 7;
+  const int b = UPPER ? (K - 1 - (int)blockIdx.x) : (int)blockIdx.x;
+  const size_t rb = (size_t)b * LU_NB;
+  const float* Db = Dinv + (size_t)b * 2 * LU_NB * LU_NB + (UPPER ? LU_NB * LU_NB : 0);
+  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+    int rr = idx & (LU_NB - 1), c = idx >> 7;
+    Ds[c * (LU_NB + 1) + rr] = Db[rr + (size_t)c * LU_NB];
+  }
+  if (t == 0) ok = 1;
+  float acc = (half == 0) ? r[rb + row] : 0.f;
+  const int nj = UPPER ? (K - 1 - b) : b;
+  for (int s = 0; s < nj; ++s) {
+    const int j = UPPER ? (K - 1 - s) : s;
+    // prefetch this thread's 64 coefficients of block (b, j) before waiting
+    float pre[LU_NB / 2];
+    const float* P = A + (rb + row) + ((size_t)j * LU_NB + half * (LU_NB / 2)) * ld;
+#pragma unroll
+    for (int q = 0; q < LU_NB / 2; ++q) pre[q] = P[(size_t)q * ld];
+    if (t == 0) {
+      int it = 0;
+      while (ld_acquire(flags + j) != epoch) {
+        if (++it > (1 << 20)) { ok = 0; atomicExch(err, 1); break; }
+        __nanosleep(64);
+      }
+    }
+    __syncthreads();
+    if (!ok) return;
+    if (t < LU_NB) ys[t] = __ldcg(y + (size_t)j * LU_NB + t);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < LU_NB / 2; ++q) acc -= pre[q] * ys[half * (LU_NB / 2) + q];
+    __syncthreads();
+  }
+  part[half][row] = acc;
+  __syncthreads();
+  if (t < LU_NB) ys[t] = part[0][t] + part[1][t];
+  __syncthreads();
+  // y_b = D_b * (r_b - ...)
+  float o = 0.f;
+#pragma unroll 16
+  for (int q = half * (LU_NB / 2); q < (half + 1) * (LU_NB / 2); ++q) o += Ds[q * (LU_NB + 1) + row] * ys[q];
+  part[half][row] = o;
+  __syncthreads();
+  if (t < LU_NB) y[rb + t] = part[0][t] + part[1][t];
+  __threadfence();
+  __syncthreads();
+  if (t == 0) st_release(flags + b, epoch);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 vector kernels of the refinement loop
+// ---------------------------------------------------------------------------
+// y = b - A x (FP64), one warp per 4 rows... simple row-parallel version:
+// each thread owns rows; A column-major so threads read consecutive rows.
+__global__ void k_residual64(const double* __restrict__ A, int64_t lda, int N,
+                             const double* __restrict__ x, const double* __restrict__ b,
+                             double* __restrict__ r, int col_chunk) {
+  // 2-D split: blockIdx.y picks a column chunk, partial sums added atomically
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * col_chunk;
+  const int c1 = min(N, c0 + col_chunk);
+  if (i >= N) return;
+  double acc = 0.0;
+  for (int c = c0; c < c1; ++c) acc = fma(A[i + (size_t)c * lda], x[c], acc);
+  if (blockIdx.y == 0) acc = b[i] - acc;
+  else acc = -acc;
+  atomicAdd(r + i, acc);
+}
+
+__global__ void k_gemv64(const double* __restrict__ A, int64_t lda, int N,
+                         const double* __restrict__ x, double* __restrict__ y, int col_chunk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c0 = blockIdx.y * col_chunk;
+  const int c1 = min(N, c0 + col_chunk);
+  if (i >= N) return;
+  double acc = 0.0;
+  for (int c = c0; c < c1; ++c) acc = fma(A[i + (size_t)c * lda], x[c], acc);
+  atomicAdd(y + i, acc);
+}
+
+// h[j] = sum_i V[i, j] w[i] for j < m  (V column-major, ld = N)
+__global__ void k_dots(const double* __restrict__ V, int64_t ldv, int N, int m,
+                       const double* __restrict__ w, double* __restrict__ h) {
+  const int j = blockIdx.x;
+  if (j >= m) return;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) acc = fma(V[i + (size_t)j * ldv], w[i], acc);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double s[32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) r += s[q];
+    h[j] = r;
+  }
+}
+
+// w -= V[:, 0:m] h ; out[i] = w (FP64)
+__global__ void k_sub_vh(const double* __restrict__ V, int64_t ldv, int N, int m,
+                         const double* __restrict__ h, double* __restrict__ w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double acc = w[i];
+    for (int j = 0; j < m; ++j) acc = fma(-V[i + (size_t)j * ldv], h[j], acc);
+    w[i] = acc;
+  }
+}
+
+// x += Z[:, 0:m] y
+__global__ void k_add_zy(const double* __restrict__ Z, int64_t ldz, int N, int m,
+                         const double* __restrict__ y, double* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double acc = x[i];
+    for (int j = 0; j < m; ++j) acc = fma(Z[i + (size_t)j * ldz], y[j], acc);
+    x[i] = acc;
+  }
+}
+
+__global__ void k_scale_copy(const double* __restrict__ w, double s, double* __restrict__ v, int N) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) v[i] = w[i] * s;
+}
+
+// FP64 -> FP32 padded vector
+__global__ void k_to_f32(const double* __restrict__ v, int N, int Npad, float* __restrict__ o) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Npad; i += gridDim.x * blockDim.x)
+    o[i] = i < N ? (float)v[i] : 0.f;
+}
+
+// z = cs .* y (FP32 -> FP64)
+__global__ void k_from_f32_scale(const float* __restrict__ y, const double* __restrict__ cs, int N,
+                                 double* __restrict__ z) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    z[i] = (double)y[i] * cs[i];
+}
+
+// ---------------------------------------------------------------------------
+// host-side sequences
+// ---------------------------------------------------------------------------
+void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, float* A32, int64_t ld32,
+                cudaStream_t st) {
+  k_colscale<<<N, 256, 0, st>>>(A64, lda, N, cs);
+  dim3 grid((Npad + 255) / 256, Npad);
+  k_scale_convert<<<grid, 256, 0, st>>>(A64, lda, N, Npad, cs, A32, ld32);
+}
+
+static void lu_attrs() {
+  static bool attr = false;
+  if (attr) return;
+  attr = true;
+  cudaFuncSetAttribute(k_diag_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(float) * 3 * LU_NB * DLD));
+  cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(float) * LU_NB * DLD));
+  cudaFuncSetAttribute(k_gemm_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)gemm_mma_smem());
+  cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)gemm_mma_smem());
+}
+
+// diagonal block k and its two panels: U12 = Linv A12, L21 = A21 Uinv
+static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, int k,
+                            cudaStream_t st) {
+  const size_t kk = (size_t)k * LU_NB;
+  const int rem = Npad - (int)kk - LU_NB;
+  k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A, ld, k, Dinv, info);
+  if (rem <= 0) return;
+  const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  const float* Ui = Li + LU_NB * LU_NB;
+  float* A12 = A + kk + (kk + LU_NB) * ld;
+  float* A21 = A + (kk + LU_NB) + kk * ld;
+  gemm_tile128(Li, LU_NB, A12, ld, A12, ld, LU_NB, rem, 1.f, 0.f, x3, st);
+  gemm_tile128(A21, ld, Ui, LU_NB, A21, ld, rem, LU_NB, 1.f, 0.f, x3, st);
+}
+
+int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
+              const TcPlan* tc, int* err) {
+  const int K = Npad / LU_NB;
+  lu_attrs();
+  for (int k = 0; k < K; ++k) {
+    const size_t kk = (size_t)k * LU_NB;
+    const int rem = Npad - (int)kk - LU_NB;
+    diag_and_panels(A, ld, Npad, Dinv, info, x3, k, st);
+    if (rem <= 0) break;
+    float* A12 = A + kk + (kk + LU_NB) * ld;
+    float* A21 = A + (kk + LU_NB) + kk * ld;
+    float* A22 = A + (kk + LU_NB) + (kk + LU_NB) * ld;
+    // A22 -= L21 * U12
+    if (tc && tc->ok && x3) {
+      tc_split(*tc, k, st);
+      int e = tc_gemm_sub(*tc, k, 0, 0, rem, rem, err, st);
+      if (e) return e;
+    } else {
+      gemm_tile128(A21, ld, A12, ld, A22, ld, rem, rem, -1.f, 1.f, x3, st);
+    }
+  }
+  return (int)cudaGetLastError();
+}
+
+// Lookahead-1 schedule on two streams.  `la` (the critical path) finishes
+// the thin part of step k's update -- block column k+1 and block row k+1 --
+// then factors diagonal block k+1, its panels and split parts; `st` runs the
+// bulk of step k's trailing update meanwhile.  evP[k]: panels/splits of step
+// k ready; evT[k]: bulk update of step k done.  tc[2]: plans with separate
+// lo/transposed buffers for even and odd steps.
+int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
+                        cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
+                        const TcPlan* tc, int* err) {
+  const int K = Npad / LU_NB;
+  lu_attrs();
+  cudaEventRecord(fork, st);
+  cudaStreamWaitEvent(la, fork, 0);
+  diag_and_panels(A, ld, Npad, Dinv, info, 1, 0, la);
+  if (K > 1) tc_split(tc[0], 0, la);
+  cudaEventRecord(evP[0], la);
+  for (int k = 0; k + 1 < K; ++k) {
+    const int rem = Npad - (k + 1) * LU_NB;
+    const TcPlan& P = tc[k & 1];
+    if (k >= 1) cudaStreamWaitEvent(la, evT[k - 1], 0);
+    int e = tc_gemm_sub(P, k, 0, 0, rem, LU_NB, err, la);  // block column k+1
+    if (!e && rem > LU_NB) e = tc_gemm_sub(P, k, 0, LU_NB, LU_NB, rem - LU_NB, err, la);  // block row
+    if (e) return e;
+    diag_and_panels(A, ld, Npad, Dinv, info, 1, k + 1, la);
+    if (k + 2 < K) tc_split(tc[(k + 1) & 1], k + 1, la);
+    cudaEventRecord(evP[k + 1], la);
+    cudaStreamWaitEvent(st, evP[k], 0);
+    if (rem > LU_NB) {
+      e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
+      if (e) return e;
+    }
+    cudaEventRecord(evT[k], st);
+  }
+  cudaStreamWaitEvent(st, evP[K - 1], 0);
+  return (int)cudaGetLastError();
+}
+
+// y = (L U)^{-1} r in place on a padded FP32 vector
+static void lu_solve_vec_steps(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
+                  cudaStream_t st) {
+  const int K = Npad / LU_NB;
+  // forward: L y = r (unit lower)
+  for (int k = 0; k < K; ++k) {
+    const size_t kk = (size_t)k * LU_NB;
+    const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+    k_blk_apply<<<1, LU_NB, 0, st>>>(Li, r + kk, tmp);
+    cudaMemcpyAsync(r + kk, tmp, sizeof(float) * LU_NB, cudaMemcpyDeviceToDevice, st);
+    const int rows = Npad - (int)kk - LU_NB;
+    if (rows > 0)
+      k_panel_gemv<<<(rows + 255) / 256, 256, 0, st>>>(A + kk + LU_NB + kk * ld, ld, rows, r + kk,
+                                                       r + kk + LU_NB);
+  }
+  // backward: U x = y
+  for (int k = K - 1; k >= 0; --k) {
+    const size_t kk = (size_t)k * LU_NB;
+    const float* Ui = Dinv + (size_t)k * 2 * LU_NB * LU_NB + LU_NB * LU_NB;
+    k_blk_apply<<<1, LU_NB, 0, st>>>(Ui, r + kk, tmp);
+    cudaMemcpyAsync(r + kk, tmp, sizeof(float) * LU_NB, cudaMemcpyDeviceToDevice, st);
+    if (kk > 0)
+      k_panel_gemv<<<((int)kk + 255) / 256, 256, 0, st>>>(A + kk * ld, ld, (int)kk, r + kk, r);
+  }
+}
+
+// y = (L U)^{-1} r on a padded FP32 vector.  r is overwritten with the
+// forward result; the solution lands in `out`.  flags: 2K ints of scratch.
+int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
+                 float* out, int* flags, int* err, cudaStream_t st) {
+  const int K = Npad / LU_NB;
+  static int max_coresident = -1;
+  if (max_coresident < 0) {
+    int dev = 0, nsm = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int dsm = (int)(sizeof(float) * LU_NB * (LU_NB + 1));
+    cudaFuncSetAttribute(k_trsv_wave<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm);
+    cudaFuncSetAttribute(k_trsv_wave<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trsv_wave<false>, 256, dsm);
+    max_coresident = nsm * per;
+  }
+  const size_t dsm = sizeof(float) * LU_NB * (LU_NB + 1);
+  if (K > max_coresident) {  // too many block rows to keep resident: step-wise launches
+    lu_solve_vec_steps(A, ld, Npad, Dinv, r, tmp, st);
+    cudaMemcpyAsync(out, r, sizeof(float) * Npad, cudaMemcpyDeviceToDevice, st);
+    return 0;
+  }
+  cudaMemsetAsync(flags, 0, sizeof(int) * 2 * K, st);
+  int epoch = 1;
+  int* f0 = flags;
+  int* f1 = flags + K;
+  float* yfwd = r;  // forward result written in place (blocks only read their own r_b before)
+  {
+    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&r, (void*)&tmp,
+                    (void*)&f0, (void*)&epoch, (void*)&err};
+    // forward: r -> tmp (separate output so that no CTA reads a block another rewrote)
+    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, dim3(K), dim3(256), args,
+                                                dsm, st);
+    if (e != cudaSuccess) return (int)e;
+  }
+  (void)yfwd;
+  {
+    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&tmp, (void*)&out,
+                    (void*)&f1, (void*)&epoch, (void*)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, dim3(K), dim3(256), args,
+                                                dsm, st);
+    if (e != cudaSuccess) return (int)e;
+  }
+  return 0;
+}
+
+void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
+                cudaStream_t st) {
+  cudaMemsetAsync(r, 0, sizeof(double) * N, st);
+  const int chunk = 512;
+  dim3 grid((N + 127) / 128, (N + chunk - 1) / chunk);
+  k_residual64<<<grid, 128, 0, st>>>(A, lda, N, x, b, r, chunk);
+}
+
+void gemv64(const double* A, int64_t lda, int N, const double* x, double* y, cudaStream_t st) {
+  cudaMemsetAsync(y, 0, sizeof(double) * N, st);
+  const int chunk = 512;
+  dim3 grid((N + 127) / 128, (N + chunk - 1) / chunk);
+  k_gemv64<<<grid, 128, 0, st>>>(A, lda, N, x, y, chunk);
+}
+
+void dots64(const double* V, int64_t ldv, int N, int m, const double* w, double* h, cudaStream_t st) {
+  k_dots<<<m, 512, 0, st>>>(V, ldv, N, m, w, h);
+}
+void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, double* w, cudaStream_t st) {
+  k_sub_vh<<<(N + 255) / 256, 256, 0, st>>>(V, ldv, N, m, h, w);
+}
+void add_zy64(const double* Z, int64_t ldz, int N, int m, const double* y, double* x, cudaStream_t st) {
+  k_add_zy<<<(N + 255) / 256, 256, 0, st>>>(Z, ldz, N, m, y, x);
+}
+void scale_copy64(const double* w, double s, double* v, int N, cudaStream_t st) {
+  k_scale_copy<<<(N + 255) / 256, 256, 0, st>>>(w, s, v, N);
+}
+void to_f32(const double* v, int N, int Npad, float* o, cudaStream_t st) {
+  k_to_f32<<<(Npad + 255) / 256, 256, 0, st>>>(v, N, Npad, o);
+}
+void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStream_t st) {
+  k_from_f32_scale<<<(N + 255) / 256, 256, 0, st>>>(y, cs, N, z);
+}
+
+}  // namespace bem

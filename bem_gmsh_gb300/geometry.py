@@ -325,12 +325,15 @@ def star_domain(ne: int, p: int = 2, seed: int = 0, amp: float = 0.08,
     th = 2 * np.pi * (np.arange(ne)[:, None] + np.arange(p + 1)[None, :] / p) / ne
     rad = r(th)
     cad = np.stack([rad * np.cos(th), rad * np.sin(th)], axis=-1)
-    dad = from_cad(f"star{seed}", cad, p, props, np.ones((ne, 1), np.int32), np.zeros((ne, 1)),
+    nd = props.ndof
+    dad = from_cad(f"star{seed}", cad, p, props, np.ones((ne, nd), np.int32), np.zeros((ne, nd)),
                    region=np.zeros(ne))
     if pontointerno:
         rr = 0.5 * r(np.linspace(0, 2 * np.pi, 16, endpoint=False))
         tt = np.linspace(0, 2 * np.pi, 16, endpoint=False)
         dad.set_internal_nodes(np.stack([rr * np.cos(tt), rr * np.sin(tt)], axis=1))
+    if nd != 1:
+        return dad  # traction-free; callers set their own data
     ana = ana_laplace_expcos(props.k)
     dirichlet_elem = th[:, 0] < np.pi
     dmask = np.repeat(dirichlet_elem, p + 1)

@@ -44,6 +44,9 @@ extern "C" {
 #define BEM_MEM_HOST 0
 #define BEM_MEM_DEVICE 1
 
+/* context options (bem_ctx_set_option) */
+#define BEM_OPT_TCGEN05 1 /* 1 (default): LU trailing updates on tcgen05; 0: legacy mma.sync */
+
 /* solve modes */
 #define BEM_SOLVE_FP64 0  /* FP64 assembly + FP64 LU */
 #define BEM_SOLVE_MIXED 1 /* FP64 A for the residual, TF32 LU, FP64 GMRES-IR */
@@ -130,6 +133,46 @@ int bem_assemble_kelvin2d(bem_ctx* ctx, const bem_geom2d* geom, double mu, doubl
 int bem_assemble_system2d(bem_ctx* ctx, const bem_geom2d* geom, int kind, double prm0,
                           double prm1, const int32_t* BC, const double* BV, int npg,
                           double near_factor, int mem, double* A, int64_t lda, double* b);
+
+/*
+ * Solve a dense FP64 system A x = b (the seam `bem_linsolve(A, b)`,
+ * src/Core/LinearSolveUtils.jl:44-49, that `solve` calls,
+ * src/Core/Solver.jl:57 and :125).  n x n, column-major, lda >= n.
+ *   BEM_SOLVE_MIXED: columns equilibrated, FP32 copy factored by a blocked
+ *     LU without pivoting whose updates run on TF32 tensor cores (3xTF32
+ *     split), then FP64 restarted GMRES on the FP64 matrix, preconditioned
+ *     by that LU, until ||b - A x|| <= tol ||b|| or max_iter iterations
+ *     (then BEM_ERR_NOT_CONVERGED with x the last iterate).  A is not
+ *     modified.
+ *   BEM_SOLVE_FP64: LU with partial pivoting in FP64 (cuSOLVER getrf/getrs,
+ *     the FP64 comparison path).
+ * stats may be NULL.
+ */
+int bem_solve_system(bem_ctx* ctx, int64_t n, const double* A, int64_t lda, const double* b,
+                     int mode, double tol, int max_iter, int mem, double* x,
+                     bem_solve_stats* stats);
+
+/*
+ * `assemble!` + `solve` in one call: the fused assembly of
+ * bem_assemble_system2d followed by bem_solve_system's solve.  x (length
+ * dof*nt) is the solution of A x = b; `split_sol!` (src/Core/Solver.jl:88-98,
+ * 133-146) maps it to (T, q) or (u, traction) from BC/BV.
+ */
+int bem_solve2d(bem_ctx* ctx, const bem_geom2d* geom, int kind, double prm0, double prm1,
+                const int32_t* BC, const double* BV, int npg, double near_factor, int mode,
+                double tol, int max_iter, int mem, double* x, bem_solve_stats* stats);
+
+/* Set a context option (BEM_OPT_*). */
+int bem_ctx_set_option(bem_ctx* ctx, int option, int value);
+
+/*
+ * Built-in consistency check of the tensor-core paths (no reference
+ * counterpart).  which = 1: factor an n x n test matrix (n a multiple of 128)
+ * once with the tcgen05 trailing updates and once with the legacy mma.sync
+ * updates; out[0] = max |difference of the factors|, out[1] = max |factor|,
+ * out[2], out[3] = factorization times in ms (tcgen05, legacy).
+ */
+int bem_selftest(bem_ctx* ctx, int which, int n, double* out);
 
 #ifdef __cplusplus
 }

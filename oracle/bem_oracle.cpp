@@ -1107,7 +1107,8 @@ void setup_ctx(Ctx& C, const Geom* g, int npg) {
 
 // H_G_full_direct scalar (Assembly_full.jl:61-85, 354-390, 801-810) and
 // vectorial (120-175, 777-787, 812-822).
-void assemble(Ctx& C, double near_factor, int nthreads, double* H, double* Gm) {
+void assemble(Ctx& C, double near_factor, int nthreads, double* H, double* Gm,
+              const uint8_t* fixed_mask = nullptr) {
   const Geom& G = *C.g;
   const int nn = G.p + 1;
   const int dof = C.prob.kind == 0 ? 1 : 2;
@@ -1127,7 +1128,8 @@ void assemble(Ctx& C, double near_factor, int nthreads, double* H, double* Gm) {
     for (int e = 0; e < G.ne; ++e) {
       for (int k = 0; k < nn; ++k) xg[k] = V2{G.px[e * nn + k], G.py[e * nn + k]};
       bool on = (i >= e * nn && i < (e + 1) * nn);
-      bool nr = near_element(pf, xg, nn, G.elen[e], near_factor);
+      bool nr = fixed_mask ? (fixed_mask[(int64_t)i * G.ne + e] != 0)
+                           : near_element(pf, xg, nn, G.elen[e], near_factor);
       if (C.prob.kind == 0) nr = nr || on;
       if (nr) {
         integrate_element(C, e, pf, i, hl.data(), gl.data());
@@ -1195,9 +1197,12 @@ static Geom to_geom(const OrcGeom* o) {
 }
 
 // kind 0: Laplace (prm0 = k); kind 1: Kelvin (prm0 = mu, prm1 = effective nu).
+// mask: optional nt x ne near classification to use instead of the test
+// (holds the near/far split fixed, e.g. to measure the integrals' rounding
+// sensitivity without classification flips).
 int orc_assemble(const OrcGeom* og, int kind, double prm0, double prm1, int npg,
                  double near_factor, int nearfield, int singular, int nthreads, double* H,
-                 double* G) {
+                 double* G, const uint8_t* mask) {
   if (!og || og->p < 1 || og->p > 8 || og->ngeo > 12 || npg < 1) return 1;
   Geom g = to_geom(og);
   Ctx C;
@@ -1207,7 +1212,7 @@ int orc_assemble(const OrcGeom* og, int kind, double prm0, double prm1, int npg,
   else { C.prob.mu = prm0; C.prob.nu = prm1; }
   C.nearfield = nearfield;
   C.singular = singular;
-  assemble(C, near_factor, nthreads, H, G);
+  assemble(C, near_factor, nthreads, H, G, mask);
   return 0;
 }
 

@@ -45,7 +45,8 @@ def lib():
         d = ctypes.c_double
         P = ctypes.POINTER(d)
         i = ctypes.c_int
-        _lib.orc_assemble.argtypes = [ctypes.POINTER(OrcGeom), i, d, d, i, d, i, i, i, P, P]
+        _lib.orc_assemble.argtypes = [ctypes.POINTER(OrcGeom), i, d, d, i, d, i, i, i, P, P,
+                                      ctypes.c_void_p]
         _lib.orc_assemble.restype = i
         _lib.orc_integrate_element.argtypes = [ctypes.POINTER(OrcGeom), i, d, d, i, i, i, i, d, d, i, P, P]
         _lib.orc_near_mask.argtypes = [ctypes.POINTER(OrcGeom), d, ctypes.POINTER(ctypes.c_uint8)]
@@ -102,8 +103,9 @@ def _props(dad):
 
 
 def assemble(dad, npg=20, near_factor=1.5, nearfield="tanp3c", singular="guiggiani", threads=0,
-             store=True):
-    """Dense FP64 H, G (H_G_full_direct, src/Core/Assembly_full.jl:61-175)."""
+             store=True, mask=None):
+    """Dense FP64 H, G (H_G_full_direct, src/Core/Assembly_full.jl:61-175).
+    `mask` (nt x ne uint8) fixes the near/far split instead of testing it."""
     L = lib()
     g, keep = make_geom(dad)
     kind, a, b = _props(dad)
@@ -111,8 +113,10 @@ def assemble(dad, npg=20, near_factor=1.5, nearfield="tanp3c", singular="guiggia
     cols = dad.ndof * dad.n
     H = np.zeros((rows, rows), order="F")
     G = np.zeros((rows, cols), order="F")
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
     rc = L.orc_assemble(ctypes.byref(g), kind, a, b, npg, float(near_factor), NEARFIELD[nearfield],
-                        1 if singular == "telles" else 0, threads, _p(H), _p(G))
+                        1 if singular == "telles" else 0, threads, _p(H), _p(G),
+                        None if m is None else m.ctypes.data)
     if rc != 0:
         raise ValueError(f"oracle assemble failed ({rc})")
     if store:

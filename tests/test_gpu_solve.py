@@ -1,0 +1,107 @@
+"""GPU solve parity: mixed precision (FP32 tensor-core LU + FP64 GMRES) and
+the FP64 comparison path, against FP64 LAPACK solves of the oracle systems.
+Bar: refined solution within 1e-10 relative of the FP64 solution of the same
+system; rel_error against the analytic field no worse than the oracle's."""
+import numpy as np
+import pytest
+
+from bem_gmsh_gb300 import (quadrado, star_domain, quadrado_elasticity, Elasticity,
+                            ana_laplace_linear, attach_analytical, ana_elasticity_patch,
+                            apply_analytical_bc, rel_error, rel_error_flux)
+from bem_gmsh_gb300.api import solve, solve_system, assemble_system
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("n", [7, 128, 300, 1000])
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_solve_system_dense(n, mode):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)) / np.sqrt(n) + 2.0 * np.eye(n)
+    A *= rng.uniform(0.1, 10.0, size=n)[None, :]  # uneven column scales
+    A = np.asfortranarray(A)
+    b = rng.standard_normal(n)
+    x, st = solve_system(A, b, mode=mode)
+    xr = np.linalg.solve(A, b)
+    assert rel(x, xr) < 1e-12, (rel(x, xr), st)
+
+
+def test_solve_system_device_pointers():
+    import torch
+    rng = np.random.default_rng(3)
+    n = 513
+    A = np.asfortranarray(rng.standard_normal((n, n)) / np.sqrt(n) + 3 * np.eye(n))
+    b = rng.standard_normal(n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().t()  # column-major view
+    bt = torch.from_numpy(b).cuda()
+    x, st = solve_system(At, bt)
+    assert rel(x.cpu().numpy(), np.linalg.solve(A, b)) < 1e-12
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_quadrado_pipeline(orc, mode):
+    dad = quadrado(ndiv=20, pontointerno=True)
+    attach_analytical(dad, ana_laplace_linear())
+    ref = quadrado(ndiv=20, pontointerno=True)
+    attach_analytical(ref, ana_laplace_linear())
+    orc.assemble(ref, npg=20)
+    orc.solve(ref)
+    solve(dad, npg=20, mode=mode)
+    assert rel(dad.cache["x"], ref.cache["x"]) < 1e-10
+    assert rel_error(dad) <= rel_error(ref) * (1 + 1e-6) + 1e-12
+    assert rel_error(dad) < 0.05
+
+
+@pytest.mark.parametrize("ne", [300, 1100])
+def test_star_pipeline_mixed(orc, ne):
+    dad = star_domain(ne, p=2, seed=11)
+    A, b = assemble_system(dad, npg=16)
+    x_fp64 = np.linalg.solve(A, b)
+    T, st = solve(dad, npg=16, mode="mixed", return_stats=True)
+    # solver parity on the same system
+    assert rel(dad.cache["x"], x_fp64) < 1e-10, st
+    # end-to-end against the oracle's assembly + LAPACK solve, within the
+    # reference algorithm's own 1-ulp geometry sensitivity (near/far split
+    # held fixed; see test_gpu_assembly.py)
+    from test_gpu_assembly import perturbed
+    ref = star_domain(ne, p=2, seed=11)
+    orc.assemble(ref, npg=16)
+    orc.solve(ref)
+    pert = perturbed(ref)
+    m = orc.near_mask(ref)
+    Hp, Gp = orc.assemble(pert, npg=16, store=False, mask=m)
+    Ap, bp = orc.apply_bc(ref, Hp, Gp)
+    sens = rel(orc.lu_solve(Ap, bp), ref.cache["x"])
+    bar = max(1e-10, 10 * sens)
+    assert rel(dad.cache["x"], ref.cache["x"]) < bar, sens
+    from bem_gmsh_gb300.geometry import analytical
+    scale = np.linalg.norm(ref.cache["x"]) / np.linalg.norm(analytical(ref))
+    assert abs(rel_error(dad) - rel_error(ref)) <= bar * scale + 1e-12
+    assert st["rel_residual"] <= 1e-14
+
+
+def test_kelvin_patch_pipeline(orc):
+    dad = quadrado_elasticity(ndiv=9, props=Elasticity(1.0, 0.3, 1.0))
+    ana = ana_elasticity_patch(E=1.0, nu=0.3, exx=0.01)
+    apply_analytical_bc(dad, ana, neumann_nodes=np.arange(0, dad.n // 2))
+    ref = quadrado_elasticity(ndiv=9, props=Elasticity(1.0, 0.3, 1.0))
+    apply_analytical_bc(ref, ana, neumann_nodes=np.arange(0, ref.n // 2))
+    orc.assemble(ref, npg=12)
+    orc.solve(ref)
+    solve(dad, npg=12, mode="mixed")
+    assert rel(dad.cache["x"], ref.cache["x"]) < 1e-10
+    assert rel_error_flux(dad) < 0.15 and rel_error(dad) < 0.15
+
+
+def test_solve_bad_args():
+    from bem_gmsh_gb300._lib import BemError
+    dad = quadrado(ndiv=5)
+    with pytest.raises(KeyError):
+        solve(dad, mode="fp16")
+    A = np.asfortranarray(np.eye(4))
+    with pytest.raises(BemError):
+        solve_system(A, np.ones(4), tol=-1.0)
