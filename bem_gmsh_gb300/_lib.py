@@ -15,6 +15,8 @@ BEM_F32, BEM_F64 = 32, 64
 BEM_MEM_HOST, BEM_MEM_DEVICE = 0, 1
 BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
 BEM_OPT_TCGEN05 = 1
+BEM_OPT_KERNEL_TIMING = 2
+KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total"]
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "refinement did not converge", 5: "device wait timed out", 6: "unsupported"}
@@ -80,6 +82,8 @@ def load(build_if_missing: bool = False):
                               ctypes.POINTER(BemSolveStats)], ctypes.c_int),
         "bem_ctx_set_option": ([ctx_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "bem_selftest": ([ctx_p, ctypes.c_int, ctypes.c_int, PD], ctypes.c_int),
+        "bem_kernel_times": ([ctx_p, PD, ctypes.POINTER(I64), ctypes.c_int], ctypes.c_int),
+        "bem_launch_count": ([], I64),
     }
     for name, (args, res) in {**sig, **optional}.items():
         if not hasattr(L, name):
@@ -117,6 +121,17 @@ class Context:
         out = (ctypes.c_double * 4)()
         self.check(self.L.bem_selftest(self.h, 1, n, out), "selftest")
         return tuple(out)
+
+    def kernel_times(self):
+        """{class: (ms, groups)} since the last call (needs BEM_OPT_KERNEL_TIMING)."""
+        n = len(KERNEL_CLASSES)
+        ms = (ctypes.c_double * n)()
+        cnt = (I64 * n)()
+        self.check(self.L.bem_kernel_times(self.h, ms, cnt, n), "kernel_times")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
+
+    def launch_count(self) -> int:
+        return int(self.L.bem_launch_count())
 
     def set_stream(self, stream_ptr: int):
         self.check(self.L.bem_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")

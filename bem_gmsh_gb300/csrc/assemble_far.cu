@@ -22,6 +22,7 @@
 // `applyBC` (src/Core/Boundary_conditions.jl:54-75, 152-174) fused in: A and b.
 #include "bem_device.cuh"
 #include "bem_kernels.h"
+#include "bem_prof.h"
 
 namespace bem {
 
@@ -448,7 +449,10 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fa.status = q.counters + 1;
   constexpr int SPT = RPT / DOF;
   dim3 grid((g.nt + 32 * SPT - 1) / (32 * SPT), (g.ne + 31) / 32);
-  far_kernel<NC, PREC, FUSED><<<grid, 256, 0, st>>>(fa);
+  {
+    KScope ks(st, KC_FAR);
+    far_kernel<NC, PREC, FUSED><<<grid, 256, 0, st>>>(fa);
+  }
 
   NearArgs na{};
   na.g = g; na.R = q.R; na.ph = q.ph; na.near_factor = q.near_factor;
@@ -462,7 +466,11 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fi.nt = g.nt; fi.n = g.n; fi.ld = q.ld; fi.H = q.H; fi.A32 = q.A32;
   fi.bc = q.bc; fi.bv = q.bv; fi.b = q.b; fi.rowsum = q.rowsum; fi.gdiag = q.gdiag;
   fi.mode = na.mode;
-  launch_near(na, fi, NC, g.nt, g.n, st);
+  {
+    KScope ks(st, KC_NEAR);
+    launch_near(na, fi, NC, g.nt, g.n, st);
+  }
+  count_launches(g.n > 0 ? 8 : 7);
 }
 
 int launch_assembly(const AsmRequest& q, cudaStream_t st) {

@@ -11,6 +11,11 @@
 #include "bem_abi_internal.h"
 #include "bem_kernels.h"
 
+namespace bem {
+std::atomic<long long> g_launches{0};
+thread_local KProf* tl_prof = nullptr;
+}  // namespace bem
+
 using bem::AsmRequest;
 using bem::GeomDev;
 using bem::Physics;
@@ -176,6 +181,7 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   cudaStreamSynchronize(c->stream);
   for (auto& b : c->slots)
     if (b.p) cudaFree(b.p);
+  c->prof.release();
   for (auto e : c->events) cudaEventDestroy(e);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
@@ -308,6 +314,7 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
 static int assemble_hg(bem_ctx* c, const bem_geom2d* g, const Physics& ph, int npg, double nf,
                        int dtype, int mem, void* H, int64_t ldh, void* G, int64_t ldg) {
   if (!c) return BEM_ERR_INVALID;
+  CallScope cs(c);
   int rc = bem_check_geom(g, npg, nf);
   if (rc) return rc;
   if (dtype != BEM_F32 && dtype != BEM_F64) return BEM_ERR_INVALID;
@@ -412,6 +419,7 @@ extern "C" int bem_assemble_system2d(bem_ctx* c, const bem_geom2d* g, int kind, 
   if (!c || !g || !BC || !BV || !A || !b) return BEM_ERR_INVALID;
   if (kind != 0 && kind != 1) return BEM_ERR_INVALID;
   if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  CallScope cs(c);
   Physics ph{};
   ph.kind = kind;
   if (kind == 0) {
@@ -439,3 +447,19 @@ extern "C" int bem_assemble_system2d(bem_ctx* c, const bem_geom2d* g, int kind, 
   if (e != cudaSuccess) return c->cuda_fail(e, "copy A, b to host");
   return BEM_OK;
 }
+
+extern "C" int bem_kernel_times(bem_ctx* c, double* ms, int64_t* counts, int n) {
+  if (!c || n < 0) return BEM_ERR_INVALID;
+  c->prof.collect();
+  for (int i = 0; i < n; ++i) {
+    if (ms) ms[i] = i < bem::KC_COUNT ? c->prof.ms[i] : 0.0;
+    if (counts) counts[i] = i < bem::KC_COUNT ? c->prof.n[i] : 0;
+  }
+  for (int i = 0; i < bem::KC_COUNT; ++i) {
+    c->prof.ms[i] = 0.0;
+    c->prof.n[i] = 0;
+  }
+  return BEM_OK;
+}
+
+extern "C" int64_t bem_launch_count(void) { return (int64_t)bem::g_launches.load(); }

@@ -9,6 +9,7 @@
 
 #include "../../include/bem_gb300.h"
 #include "bem_kernels.h"
+#include "bem_prof.h"
 
 struct bem_ctx {
   enum Slot {
@@ -29,6 +30,7 @@ struct bem_ctx {
   Buf slots[NSLOT];
   int pair_cap_hint = 0;
   int opt_tcgen05 = 1;  // BEM_OPT_TCGEN05: trailing updates on tcgen05
+  bem::KProf prof;      // BEM_OPT_KERNEL_TIMING
 
   // second stream and events of the lookahead LU (created on first use)
   cudaStream_t la_stream = nullptr;
@@ -40,6 +42,21 @@ struct bem_ctx {
   // Grow-only device buffer for `slot` (NULL on allocation failure).
   void* get(int slot, size_t bytes);
   int cuda_fail(cudaError_t e, const char* where);
+};
+
+// Marks the context whose call runs on this thread (for kernel timing);
+// collects the timings when the call returns (all streams synchronized).
+struct CallScope {
+  bem_ctx* c;
+  explicit CallScope(bem_ctx* c_) : c(c_) { bem::tl_prof = (c && c->prof.on) ? &c->prof : nullptr; }
+  ~CallScope() {
+    if (bem::tl_prof) {
+      if (c->la_stream) cudaStreamSynchronize(c->la_stream);
+      cudaStreamSynchronize(c->stream);
+      c->prof.collect();
+    }
+    bem::tl_prof = nullptr;
+  }
 };
 
 int bem_check_geom(const bem_geom2d* g, int npg, double near_factor);

@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "bem_lu.h"
+#include "bem_prof.h"
 
 namespace bem {
 
@@ -350,6 +351,7 @@ void tc_split(const TcPlan& p, int k, cudaStream_t st) {
   if (rem <= 0) return;
   dim3 sg(rem / 32, LU_NB / 32);
   k_split_lo<<<sg, dim3(32, 8), 0, st>>>(p.A, p.ld, kk, rem, p.Lt, p.Ltlo, p.Ulo);
+  count_launches(1);
 }
 
 int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st) {
@@ -369,6 +371,7 @@ int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, 
   a.beta = 1.f;
   a.err = err;
   dim3 grid(M / tc::BM, (N + tc::BN - 1) / tc::BN);
+  count_launches(1);
   tc::k_gemm_tc<<<grid, 256, tc::SMEM_BYTES, st>>>(*(const CUtensorMap*)p.mA, *(const CUtensorMap*)p.mAlo,
                                                     *(const CUtensorMap*)p.mB, *(const CUtensorMap*)p.mBlo,
                                                     a);

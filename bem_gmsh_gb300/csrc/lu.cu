@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "bem_lu.h"
+#include "bem_prof.h"
 
 namespace bem {
 
@@ -460,6 +461,7 @@ size_t gemm_mma_smem() { return sizeof(float) * (2 * GK * ALD + 2 * 128 * BLD); 
 void gemm_tile128(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
                   int M, int N, float alpha, float beta, int x3, cudaStream_t st) {
   if (M <= 0 || N <= 0) return;
+  count_launches(1);
   dim3 grid(M / 128, N / 128);
   const size_t sm = gemm_mma_smem();
   if (x3)
@@ -666,6 +668,8 @@ __global__ void k_from_f32_scale(const float* __restrict__ y, const double* __re
 // ---------------------------------------------------------------------------
 void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, float* A32, int64_t ld32,
                 cudaStream_t st) {
+  KScope ks(st, KC_LU_PREP);
+  count_launches(2);
   k_colscale<<<N, 256, 0, st>>>(A64, lda, N, cs);
   dim3 grid((Npad + 255) / 256, Npad);
   k_scale_convert<<<grid, 256, 0, st>>>(A64, lda, N, Npad, cs, A32, ld32);
@@ -691,6 +695,7 @@ static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* in
   const size_t kk = (size_t)k * LU_NB;
   const int rem = Npad - (int)kk - LU_NB;
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A, ld, k, Dinv, info);
+  count_launches(1);
   if (rem <= 0) return;
   const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
   const float* Ui = Li + LU_NB * LU_NB;
@@ -735,6 +740,7 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
                         const TcPlan* tc, int* err) {
   const int K = Npad / LU_NB;
   lu_attrs();
+  KScope total(st, KC_LU_TOTAL);
   cudaEventRecord(fork, st);
   cudaStreamWaitEvent(la, fork, 0);
   diag_and_panels(A, ld, Npad, Dinv, info, 1, 0, la);
@@ -744,14 +750,19 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     const int rem = Npad - (k + 1) * LU_NB;
     const TcPlan& P = tc[k & 1];
     if (k >= 1) cudaStreamWaitEvent(la, evT[k - 1], 0);
-    int e = tc_gemm_sub(P, k, 0, 0, rem, LU_NB, err, la);  // block column k+1
-    if (!e && rem > LU_NB) e = tc_gemm_sub(P, k, 0, LU_NB, LU_NB, rem - LU_NB, err, la);  // block row
-    if (e) return e;
-    diag_and_panels(A, ld, Npad, Dinv, info, 1, k + 1, la);
-    if (k + 2 < K) tc_split(tc[(k + 1) & 1], k + 1, la);
+    int e;
+    {
+      KScope crit(la, KC_LU_CRIT);
+      e = tc_gemm_sub(P, k, 0, 0, rem, LU_NB, err, la);  // block column k+1
+      if (!e && rem > LU_NB) e = tc_gemm_sub(P, k, 0, LU_NB, LU_NB, rem - LU_NB, err, la);  // block row
+      if (e) return e;
+      diag_and_panels(A, ld, Npad, Dinv, info, 1, k + 1, la);
+      if (k + 2 < K) tc_split(tc[(k + 1) & 1], k + 1, la);
+    }
     cudaEventRecord(evP[k + 1], la);
     cudaStreamWaitEvent(st, evP[k], 0);
     if (rem > LU_NB) {
+      KScope trail(st, KC_LU_TRAIL);
       e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
       if (e) return e;
     }
@@ -809,6 +820,8 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
     cudaMemcpyAsync(out, r, sizeof(float) * Npad, cudaMemcpyDeviceToDevice, st);
     return 0;
   }
+  KScope ks(st, KC_TRSV);
+  count_launches(2);
   cudaMemsetAsync(flags, 0, sizeof(int) * 2 * K, st);
   int epoch = 1;
   int* f0 = flags;
@@ -835,6 +848,8 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
 
 void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
                 cudaStream_t st) {
+  KScope ks(st, KC_GEMV);
+  count_launches(1);
   cudaMemsetAsync(r, 0, sizeof(double) * N, st);
   const int chunk = 512;
   dim3 grid((N + 127) / 128, (N + chunk - 1) / chunk);
@@ -842,6 +857,8 @@ void residual64(const double* A, int64_t lda, int N, const double* x, const doub
 }
 
 void gemv64(const double* A, int64_t lda, int N, const double* x, double* y, cudaStream_t st) {
+  KScope ks(st, KC_GEMV);
+  count_launches(1);
   cudaMemsetAsync(y, 0, sizeof(double) * N, st);
   const int chunk = 512;
   dim3 grid((N + 127) / 128, (N + chunk - 1) / chunk);
@@ -849,21 +866,27 @@ void gemv64(const double* A, int64_t lda, int N, const double* x, double* y, cud
 }
 
 void dots64(const double* V, int64_t ldv, int N, int m, const double* w, double* h, cudaStream_t st) {
+  count_launches(1);
   k_dots<<<m, 512, 0, st>>>(V, ldv, N, m, w, h);
 }
 void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, double* w, cudaStream_t st) {
+  count_launches(1);
   k_sub_vh<<<(N + 255) / 256, 256, 0, st>>>(V, ldv, N, m, h, w);
 }
 void add_zy64(const double* Z, int64_t ldz, int N, int m, const double* y, double* x, cudaStream_t st) {
+  count_launches(1);
   k_add_zy<<<(N + 255) / 256, 256, 0, st>>>(Z, ldz, N, m, y, x);
 }
 void scale_copy64(const double* w, double s, double* v, int N, cudaStream_t st) {
+  count_launches(1);
   k_scale_copy<<<(N + 255) / 256, 256, 0, st>>>(w, s, v, N);
 }
 void to_f32(const double* v, int N, int Npad, float* o, cudaStream_t st) {
+  count_launches(1);
   k_to_f32<<<(Npad + 255) / 256, 256, 0, st>>>(v, N, Npad, o);
 }
 void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStream_t st) {
+  count_launches(1);
   k_from_f32_scale<<<(N + 255) / 256, 256, 0, st>>>(y, cs, N, z);
 }
 

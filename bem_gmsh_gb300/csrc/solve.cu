@@ -302,6 +302,7 @@ extern "C" int bem_solve_system(bem_ctx* c, int64_t n, const double* A, int64_t 
   if (mode != BEM_SOLVE_FP64 && mode != BEM_SOLVE_MIXED) return BEM_ERR_INVALID;
   if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
   if (!(tol > 0) || max_iter < 1) return BEM_ERR_INVALID;
+  CallScope cscope(c);
   cudaSetDevice(c->device);
   const int N = (int)n;
   if (stats) std::memset(stats, 0, sizeof(*stats));
@@ -347,6 +348,7 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   if (mode != BEM_SOLVE_FP64 && mode != BEM_SOLVE_MIXED) return BEM_ERR_INVALID;
   if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
   if (!(tol > 0) || max_iter < 1) return BEM_ERR_INVALID;
+  CallScope cscope(c);
   bem::Physics ph{};
   ph.kind = kind;
   if (kind == 0) {
@@ -394,6 +396,10 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   if (!c) return BEM_ERR_INVALID;
   if (option == BEM_OPT_TCGEN05) {
     c->opt_tcgen05 = value ? 1 : 0;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_KERNEL_TIMING) {
+    c->prof.on = value != 0;
     return BEM_OK;
   }
   return BEM_ERR_INVALID;

@@ -1,0 +1,339 @@
+#!/usr/bin/env python3
+"""Headline benchmark: dense 2-D Laplace BEM solve at N = 8193 on one GB300.
+
+Workload (the N=8192 configuration, restated as seeded synthetic geometry):
+star-shaped boundary r(t) = 1 + sum_{k=2..6} a_k cos(k t + phi_k), a_k ~
+U(0, 0.08), phi_k ~ U(0, 2 pi) (seed 0), 2731 discontinuous quadratic
+elements (N = 8193: 8192 is not a multiple of 3 nodes per element), field
+T = e^x cos y with Dirichlet data where the element starts at t in [0, pi)
+and Neumann data on [pi, 2 pi), npg = 16 near-field rule.
+
+One step = one solve: fused assembly of A x = b (far field, near-singular
+and singular integrals, boundary-condition swap) + FP32 tensor-core LU +
+FP64 GMRES refinement to ||b - A x|| <= 1e-14 ||b||.  `value` is solves/s
+with the geometry and boundary data already resident on the device; `e2e`
+is the same through the public host-buffer API (host->device copy of the
+inputs and device->host copy of x inside each step).  The FP64 comparison
+path (FP64 assembly + cuSOLVER LU) is timed on the same input.
+
+--impl reference times the CPU restatement of the reference's own path
+(assembly on all host threads + LAPACK LU), the CPU implementation of this
+path, on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("solves/sec & H+G entries/sec at N=8192, mixed vs FP64 GPU, "
+          "≤1e-10 rel err vs FP64")
+def workload(ne, npg):
+    return (f"star-shaped Laplace domain, {ne} quadratic elements, N={3 * ne} collocation nodes, "
+            f"npg={npg}, mixed Dirichlet/Neumann data for T=exp(x)cos(y), seed 0")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms in the background."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(dad_factory, steps, warmup, npg):
+    """The CPU restatement of the path: oracle assembly (all host threads) +
+    applyBC + LAPACK LU (SciPy/OpenBLAS, all threads)."""
+    from oracle import oracle as orc
+    ts = []
+    x = None
+    for it in range(warmup + steps):
+        dad = dad_factory()
+        r = orc.timed_pipeline(dad, npg=npg, threads=os.cpu_count() or 1)
+        if it >= warmup:
+            ts.append(r["total"])
+        x = r["x"]
+    return ts, x
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ne", type=int, default=2731)
+    ap.add_argument("--npg", type=int, default=16)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-samples", type=int, default=1)
+    args = ap.parse_args()
+    assert args.warmup >= 3 or args.impl == "reference" or args.warmup >= 0
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from bem_gmsh_gb300.geometry import star_domain, rel_error
+
+    def make():
+        return star_domain(args.ne, p=2, seed=0)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ts, _ = cpu_reference(make, max(1, args.steps), min(args.warmup, 1), args.npg)
+        v = 1.0 / statistics.mean(ts)
+        cores = os.cpu_count() or 1
+        line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": len(ts),
+                "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * statistics.mean(ts),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": workload(args.ne, args.npg), "N": 3 * args.ne, "npg": args.npg},
+                "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port",
+                                 "sample": f"{len(ts)} full solves of the workload (assembly on {cores} "
+                                           f"threads + LAPACK LU)"},
+                "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import numpy as np
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    from bem_gmsh_gb300 import _lib
+    from bem_gmsh_gb300.api import geom_struct, solve, split_sol
+
+    ctx = _lib.default_context(local_rank if world > 1 else 0)
+    dad = make()
+    N = dad.nt
+    # device-resident inputs
+    g, keep = geom_struct(dad, device=True)
+    BC = torch.as_tensor(np.asarray(dad.BC, np.int32)).cuda()
+    BV = torch.as_tensor(np.asarray(dad.BV, np.float64)).cuda()
+    x = torch.zeros(N, dtype=torch.float64, device="cuda")
+    st = _lib.BemSolveStats()
+
+    def step(mode):
+        rc = ctx.L.bem_solve2d(ctx.h, g, 0, float(dad.properties.k), 0.0, BC.data_ptr(), BV.data_ptr(),
+                               args.npg, 1.5, mode, 1e-14, 200, _lib.BEM_MEM_DEVICE, x.data_ptr(), st)
+        ctx.check(rc, "bem_solve2d")
+
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        step(_lib.BEM_SOLVE_MIXED)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ctx.set_option(_lib.BEM_OPT_KERNEL_TIMING, 1)
+    ctx.kernel_times()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = ctx.launch_count()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iters = []
+    for _ in range(args.steps):
+        step(_lib.BEM_SOLVE_MIXED)
+        iters.append(st.iterations)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - l0
+    clk = clocks.stop()
+    ktimes = ctx.kernel_times()
+    ctx.set_option(_lib.BEM_OPT_KERNEL_TIMING, 0)
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+    x_mixed = x.cpu().numpy().copy()
+    stats_mixed = dict(iterations=st.iterations, rel_residual=st.rel_residual,
+                       t_assemble_ms=st.t_assemble_ms, t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)
+
+    # FP64 comparison path
+    step(_lib.BEM_SOLVE_FP64)  # warm-up (library load, workspace)
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.fp64_steps):
+        step(_lib.BEM_SOLVE_FP64)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = f0.elapsed_time(f1) / args.fp64_steps
+    x64 = x.cpu().numpy().copy()
+    rel_vs_fp64 = float(np.linalg.norm(x_mixed - x64) / np.linalg.norm(x64))
+
+    # assembly throughput: H and G in FP32 (device resident)
+    ld = (N + 3) // 4 * 4
+    Hs = torch.empty((N, ld), dtype=torch.float32, device="cuda")
+    Gs = torch.empty((dad.n, ld), dtype=torch.float32, device="cuda")
+    H = Hs.t()[:N]
+    G = Gs.t()[:N]
+
+    def asm():
+        rc = ctx.L.bem_assemble_laplace2d(ctx.h, g, 1.0, args.npg, 1.5, _lib.BEM_F32, _lib.BEM_MEM_DEVICE,
+                                          H.data_ptr(), ld, G.data_ptr(), ld)
+        ctx.check(rc, "assemble")
+    for _ in range(3):
+        asm()
+    torch.cuda.synchronize()
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(args.steps):
+        asm()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    ms_asm = a0.elapsed_time(a1) / args.steps
+    entries = N * N + N * dad.n
+    entries_per_s = entries / (ms_asm * 1e-3)
+
+    # end to end through the public API (host buffers)
+    ctx.set_stream(0)
+    e2e_dad = make()
+    solve(e2e_dad, npg=args.npg, mode="mixed", ctx=ctx)
+    te = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        solve(e2e_dad, npg=args.npg, mode="mixed", ctx=ctx)
+        te.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.median(te)
+    h2d = sum(a.nbytes for a in (e2e_dad.collocation, e2e_dad.normal, e2e_dad.jacobian, e2e_dad.elem_length,
+                                 e2e_dad.geo, e2e_dad.elem_weight, e2e_dad.BC, e2e_dad.BV))
+    d2h = 8 * N
+
+    # roofline of the dominant kernel class (device time over the timed region)
+    hbm, bf16, src = peaks()
+    nb = (N + 127) // 128 * 128
+    algo = {
+        # bytes: the FP64 system matrix written once per assembly
+        "far": ("hbm", 8.0 * N * N, "GB/s"),
+        # bytes: FP64 A read + FP32 A written
+        "lu_prep": ("hbm", 12.0 * N * N, "GB/s"),
+        # flops: 2 (rem-128)^2 128 per step, summed over the factorization
+        "lu_trail": ("tensor", sum(2.0 * (nb - (k + 2) * 128) ** 2 * 128 for k in range(nb // 128 - 1)),
+                     "TFLOP/s"),
+        # bytes: one FP64 matrix read per product
+        "gemv": ("hbm", 8.0 * N * N, "GB/s"),
+    }
+    shares = {k: v[0] for k, v in ktimes.items() if k != "lu_total"}
+    dom = max((k for k in shares if k in algo), key=lambda k: shares[k])
+    bound, units_total, unit = algo[dom]
+    groups = max(1, ktimes[dom][1])
+    # per launch group: far/lu_prep once per solve, lu_trail = all steps of one LU, gemv per product
+    per_solve = {"far": 1, "lu_prep": 1, "lu_trail": None, "gemv": None}[dom]
+    t_avg_s = ktimes[dom][0] / groups * 1e-3
+    if dom == "lu_trail":
+        units = units_total / (nb // 128 - 1)  # average per step group
+    else:
+        units = units_total
+    achieved = units / t_avg_s / (1e9 if bound == "hbm" else 1e12)
+    peak = hbm if bound == "hbm" else bf16
+    roof = {"kernel_class": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "traffic": None, "peak_source": src,
+            "note": ("tensor peak is the measured dense bf16 burst; the TF32 dense rate is half of it"
+                     if bound == "tensor" else "measured copy bandwidth")}
+
+    # CPU baseline: the oracle port on the host cores, one full solve sample
+    cpu_ts, x_orc = cpu_reference(make, max(1, args.cpu_samples), 0, args.npg)
+    cores = os.cpu_count() or 1
+    cpu_v = 1.0 / statistics.mean(cpu_ts)
+    rel_vs_oracle = float(np.linalg.norm(x_mixed - x_orc) / np.linalg.norm(x_orc))
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload(args.ne, args.npg), "N": N, "npg": args.npg, "mode": "mixed (FP32/TF32 LU + FP64 GMRES)",
+                       "tol": 1e-14, "l2": "inputs larger than L2 (FP64 system 537 MB)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "entries_per_s": entries_per_s, "assembly_ms_fp32_HG": ms_asm,
+            "fp64_solves_per_s": 1e3 / ms64, "fp64_ms_per_step": ms64,
+            "speedup_mixed_vs_fp64": ms64 / ms,
+            "rel_err_vs_fp64_gpu": rel_vs_fp64, "rel_err_vs_cpu_oracle": rel_vs_oracle,
+            "rel_error_analytic": float(rel_error(e2e_dad)),
+            "gmres_iterations": iters[-1] if iters else None, "stats": stats_mixed,
+            "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()},
+            "e2e": {"value": 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roof,
+            "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(cpu_ts)} full solve(s) of the same workload: oracle assembly on "
+                                       f"{cores} threads + LAPACK LU"},
+            "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

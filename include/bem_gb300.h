@@ -45,7 +45,19 @@ extern "C" {
 #define BEM_MEM_DEVICE 1
 
 /* context options (bem_ctx_set_option) */
-#define BEM_OPT_TCGEN05 1 /* 1 (default): LU trailing updates on tcgen05; 0: legacy mma.sync */
+#define BEM_OPT_TCGEN05 1       /* 1 (default): LU trailing updates on tcgen05; 0: legacy mma.sync */
+#define BEM_OPT_KERNEL_TIMING 2 /* 1: time kernel classes with CUDA events (bem_kernel_times) */
+
+/* kernel classes reported by bem_kernel_times */
+#define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */
+#define BEM_KC_NEAR 1      /* near-singular, on-element and diagonal kernels */
+#define BEM_KC_LU_PREP 2   /* equilibration + FP32 copy */
+#define BEM_KC_LU_CRIT 3   /* LU critical path: diagonal blocks, panels, thin updates */
+#define BEM_KC_LU_TRAIL 4  /* LU bulk trailing updates (tcgen05) */
+#define BEM_KC_TRSV 5      /* triangular solves of the preconditioner */
+#define BEM_KC_GEMV 6      /* FP64 matrix-vector products and residuals */
+#define BEM_KC_LU_TOTAL 7  /* whole factorization */
+#define BEM_KC_COUNT 8
 
 /* solve modes */
 #define BEM_SOLVE_FP64 0  /* FP64 assembly + FP64 LU */
@@ -164,6 +176,14 @@ int bem_solve2d(bem_ctx* ctx, const bem_geom2d* geom, int kind, double prm0, dou
 
 /* Set a context option (BEM_OPT_*). */
 int bem_ctx_set_option(bem_ctx* ctx, int option, int value);
+
+/* Accumulated device time (ms) and launch-group counts per kernel class
+ * (BEM_KC_*) since the last call, with BEM_OPT_KERNEL_TIMING on; resets the
+ * accumulators.  Tracing facility, no reference counterpart. */
+int bem_kernel_times(bem_ctx* ctx, double* ms, int64_t* counts, int n);
+
+/* Number of kernel launches made by the library in this process. */
+int64_t bem_launch_count(void);
 
 /*
  * Built-in consistency check of the tensor-core paths (no reference
