@@ -84,6 +84,8 @@ def load(build_if_missing: bool = False):
         "bem_selftest": ([ctx_p, ctypes.c_int, ctypes.c_int, PD], ctypes.c_int),
         "bem_kernel_times": ([ctx_p, PD, ctypes.POINTER(I64), ctypes.c_int], ctypes.c_int),
         "bem_launch_count": ([], I64),
+        "bem_assemble_laplace2d_noalloc": ([ctypes.POINTER(BemGeom2D), D, ctypes.c_int, D, ctypes.c_int, VP, I64,
+                                            VP, I64, VP], ctypes.c_int),
     }
     for name, (args, res) in {**sig, **optional}.items():
         if not hasattr(L, name):

@@ -112,6 +112,10 @@ void build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) 
 
 }  // namespace
 
+void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) {
+  build_rules(g, npg, ew_host, R);
+}
+
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------

@@ -60,6 +60,8 @@ struct CallScope {
 };
 
 int bem_check_geom(const bem_geom2d* g, int npg, double near_factor);
+// host-side rule tables of an assembly (element Gauss weights on the host)
+void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, bem::Rules& R);
 int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, bem::GeomDev& gd,
                    bem::Rules& R);
 int bem_run_assembly(bem_ctx* c, bem::AsmRequest& q);

@@ -186,6 +186,30 @@ int bem_kernel_times(bem_ctx* ctx, double* ms, int64_t* counts, int n);
 int64_t bem_launch_count(void);
 
 /*
+ * Allocation-free Laplace H, G: same results as bem_assemble_laplace2d with
+ * BEM_MEM_DEVICE, for callers that cannot allocate device memory while they
+ * run (device memory owned by another allocator's pool such as CUDA.jl's or
+ * PyTorch's, real-time loops that may only allocate at start-up).  No
+ * counterpart in the reference.  It calls no cudaMalloc/cudaFree and needs
+ * no bem_ctx: the assembly scratch is a fixed device array of
+ * BEM_NOALLOC_BYTES inside the library, present on every GPU that loads the
+ * library until the process exits.  Limits: nt <= BEM_NOALLOC_MAX_NT,
+ * ne <= BEM_NOALLOC_MAX_NE, at most 24*BEM_NOALLOC_MAX_NT near pairs;
+ * larger problems return BEM_ERR_UNSUPPORTED.  geom, H and G are device
+ * pointers; work runs on cuda_stream (NULL = legacy default stream) and the
+ * call returns when it is done.  The first call on each device looks up the
+ * array's address (loading the module) and should precede any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * race, so callers must serialize them.
+ */
+#define BEM_NOALLOC_MAX_NT 16384
+#define BEM_NOALLOC_MAX_NE 8192
+#define BEM_NOALLOC_BYTES 4456704
+int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, int npg, double near_factor,
+                                   int dtype, void* H, int64_t ldh, void* G, int64_t ldg,
+                                   void* cuda_stream);
+
+/*
  * Built-in consistency check of the tensor-core paths (no reference
  * counterpart).  which = 1: factor an n x n test matrix (n a multiple of 128)
  * once with the tcgen05 trailing updates and once with the legacy mma.sync
