@@ -135,6 +135,13 @@ class Context:
     def launch_count(self) -> int:
         return int(self.L.bem_launch_count())
 
+    def selftest_diag(self, n: int = 128):
+        """Blocked vs Gauss-Jordan factorization of one 128 x 128 block:
+        (max |diff L\\U|, max |L\\U|, max |diff inverses|, max |inverse|)."""
+        out = (ctypes.c_double * 4)()
+        self.check(self.L.bem_selftest(self.h, 2, n, out), "selftest")
+        return tuple(out)
+
     def set_stream(self, stream_ptr: int):
         self.check(self.L.bem_ctx_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")
 

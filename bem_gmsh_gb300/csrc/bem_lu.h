@@ -38,6 +38,8 @@ void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStre
 void gemm_tile128(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
                   int M, int N, float alpha, float beta, int x3, cudaStream_t st);
 
+void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, int* info, cudaStream_t st);
+
 // tcgen05 trailing update (gemm_tc.cu).  The plan holds the TMA maps of the
 // transposed L panel, its lo part, the matrix (U panel) and the U lo part.
 struct TcPlan {

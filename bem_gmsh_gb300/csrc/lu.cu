@@ -58,90 +58,10 @@ __global__ void k_scale_convert(const double* __restrict__ A, int64_t lda, int N
 // ---------------------------------------------------------------------------
 constexpr int DLD = LU_NB + 1;
 
-// Gauss-Jordan form: the forward elimination applied to [A | I] leaves U in
-// A and L^{-1} in the identity part; the backward sweep on [U | I] builds
-// U^{-1} one row at a time, pushing each finished row into the rows above.
-// Every step is one block-wide barrier pair; all work inside a step is
-// spread over the 512 threads.
-__global__ void __launch_bounds__(512) k_diag_factor(float* __restrict__ A, int64_t ld, int k,
-                                                     float* __restrict__ Dinv, int* __restrict__ info) {
-  extern __shared__ float sm[];
-  float* s = sm;                    // [col][row], ld DLD: A -> L\U
-  float* li = sm + LU_NB * DLD;     // Linv, [col][row]
-  float* ui = li + LU_NB * DLD;     // Uinv, [col][row]
-  __shared__ float lcol[LU_NB];
-  __shared__ int bad;
-  const int t = threadIdx.x;
-  const size_t off = (size_t)k * LU_NB;
-  float* Ab = A + off + off * ld;
-  if (t == 0) bad = 0;
-  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
-    int r = idx & (LU_NB - 1), c = idx >> 7;
-    s[c * DLD + r] = Ab[r + (size_t)c * ld];
-    li[c * DLD + r] = (r == c) ? 1.f : 0.f;
-    ui[c * DLD + r] = 0.f;
-  }
-  __syncthreads();
-  // forward elimination on [A | I]
-  for (int j = 0; j < LU_NB; ++j) {
-    const float piv = s[j * DLD + j];
-    if (t == 0 && !(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
-    const float inv = 1.f / piv;
-    for (int r = j + 1 + t; r < LU_NB; r += blockDim.x) {
-      float l = s[j * DLD + r] * inv;
-      lcol[r] = l;
-      s[j * DLD + r] = l;  // multiplier stored as L
-    }
-    __syncthreads();
-    // columns j+1..127 of A and columns 0..j of Linv: thread owns column
-    // (t & 127) and every 4th row; conflict-free ([col][row], ld 129)
-    {
-      const int cc = t & (LU_NB - 1);
-      const int r0 = j + 1 + (t >> 7);
-      if (cc > j) {
-        const float u = s[cc * DLD + j];
-        for (int r = r0; r < LU_NB; r += 4) s[cc * DLD + r] -= lcol[r] * u;
-      } else {
-        const float u = li[cc * DLD + j];
-        for (int r = r0; r < LU_NB; r += 4) li[cc * DLD + r] -= lcol[r] * u;
-      }
-    }
-    __syncthreads();
-  }
-  // backward sweep: U X = I, rows from the bottom
-  for (int j = LU_NB - 1; j >= 0; --j) {
-    const float inv = 1.f / s[j * DLD + j];
-    // finish row j: X[j][c] = (I[j][c] - pushed terms) / u_jj for c >= j
-    for (int c = j + t; c < LU_NB; c += blockDim.x) {
-      float v = ((c == j) ? 1.f : 0.f) + ui[c * DLD + j];
-      ui[c * DLD + j] = v * inv;
-    }
-    __syncthreads();
-    // push into rows r < j: R[r][c] -= u_rj X[j][c], c >= j (accumulated in ui with sign)
-    {
-      const int c = t & (LU_NB - 1);
-      if (c >= j) {
-        const float xj = ui[c * DLD + j];
-        for (int r = t >> 7; r < j; r += 4) ui[c * DLD + r] -= s[j * DLD + r] * xj;
-      }
-    }
-    __syncthreads();
-  }
-  if (t == 0 && bad) atomicExch(info, k + 1);
-  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
-    int r = idx & (LU_NB - 1), c = idx >> 7;
-    Ab[r + (size_t)c * ld] = s[c * DLD + r];
-  }
-  float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
-  float* Ui = Li + LU_NB * LU_NB;
-  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
-    int r = idx & (LU_NB - 1), c = idx >> 7;
-    Li[r + c * LU_NB] = li[c * DLD + r];
-    Ui[r + c * LU_NB] = ui[c * DLD + r];
-  }
-}
-
-// Register-blocked version of the same Gauss-Jordan factorization.  Warp w
+// Gauss-Jordan factorization of one diagonal block, register blocked: the
+// forward elimination applied to [A | I] leaves U in A and L^{-1} in the
+// identity part; the backward sweep on [U | I] builds U^{-1}.  It is the
+// independent check of the tiled kernel below (bem_selftest).  Warp w
 // (0..15) owns rows w, w+16, ..., w+112 and lane l owns columns l, l+32,
 // l+64, l+96, so every thread holds an 8 x 4 tile of [A | I] in registers.
 // Step j publishes row j (one warp) and column j (one lane per warp) to
@@ -675,18 +595,396 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
   k_scale_convert<<<grid, 256, 0, st>>>(A64, lda, N, Npad, cs, A32, ld32);
 }
 
+// ---------------------------------------------------------------------------
+// Tiled factorization of a 128 x 128 diagonal block (no pivoting) and the
+// inverses of its unit-lower and upper triangles, all in shared memory
+// (column-major, ld 132 so that 4 consecutive rows are one 16-byte load).
+//   for each 16-wide panel p (jb = 16 p):
+//     F1  warp 0 factors the (128-jb) x 16 panel in registers (rows over
+//         lanes, pivot rows broadcast by shuffles) and inverts its 16 x 16
+//         unit-lower block;
+//     F2  one thread per column: U[jb:jb+16, c] = Linv_pp A[jb:jb+16, c];
+//     F3  trailing update A22 -= L21 U12 with 4 x 4 register tiles.
+//   then the inverses, L by warps 0-7 and U by warps 8-15 at the same time
+//   (named barriers), by recursive doubling from the 16 x 16 diagonal
+//   inverses: for halves A, B of a 2h block
+//     Linv_BA = -Linv_BB (L_BA Linv_AA),   Uinv_AB = -Uinv_AA (U_AB Uinv_BB),
+//   h = 16, 32, 64, every product on 4 x CT register tiles.
+// 24 block barriers and 9 half-block barriers per half in all.  A and ld
+// must allow 16-byte loads (ld % 4 == 0, 16-byte aligned A).
+// ---------------------------------------------------------------------------
+constexpr int DB = 16;        // panel width
+constexpr int TLD = LU_NB + 4;  // shared leading dimension of the tiled kernel
+
+__device__ __forceinline__ void half_sync(int id) {
+  asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory");
+}
+
+// acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
+// shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
+// qs, qe multiples of 4.
+template <int CT>
+__device__ __forceinline__ void tile_mm(const float* Pb, const float* Qb, int r0, int c0, int qs, int qe,
+                                        float (&acc)[4][CT]) {
+  for (int q = qs; q < qe; q += 4) {
+    float4 p[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] = *(const float4*)&Pb[(q + i) * TLD + r0];
+#pragma unroll
+    for (int j = 0; j < CT; ++j) {
+      const float4 qv = *(const float4*)&Qb[(c0 + j) * TLD + q];
+      const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        acc[0][j] = fmaf(p[i].x, qq[i], acc[0][j]);
+        acc[1][j] = fmaf(p[i].y, qq[i], acc[1][j]);
+        acc[2][j] = fmaf(p[i].z, qq[i], acc[2][j]);
+        acc[3][j] = fmaf(p[i].w, qq[i], acc[3][j]);
+      }
+    }
+  }
+}
+
+template <int CT>
+__device__ __forceinline__ void tile_store_neg(float* Ob, int r0, int c0, const float (&acc)[4][CT]) {
+#pragma unroll
+  for (int j = 0; j < CT; ++j)
+    *(float4*)&Ob[(c0 + j) * TLD + r0] = make_float4(-acc[0][j], -acc[1][j], -acc[2][j], -acc[3][j]);
+}
+
+template <int CT>
+__device__ __forceinline__ void tile_store(float* Ob, int r0, int c0, const float (&acc)[4][CT]) {
+#pragma unroll
+  for (int j = 0; j < CT; ++j)
+    *(float4*)&Ob[(c0 + j) * TLD + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+}
+
+// One doubling level of the L (upper = false) or U (upper = true) inverse
+// for half-block size h; u = thread index within the half (0..255).
+template <int H, bool UPPER>
+__device__ __forceinline__ void inv_level(const float* S, float* X, int u, int bar) {
+  constexpr int CT = H / 16;            // 1, 2, 4
+  constexpr int TR = H / 4;             // row tiles per block
+  constexpr int PER = TR * (H / CT);    // threads per pair (64, 128, 256)
+  const int pair = u / PER, rem = u % PER;
+  const int r0 = 4 * (rem % TR), c0 = CT * (rem / TR);
+  const int o = pair * 2 * H;           // offset of the 2h block
+  float acc[4][CT] = {};
+  if (!UPPER) {
+    // T = L_BA Linv_AA -> X_BA slot
+    tile_mm<CT>(S + o * TLD + o + H, X + o * TLD + o, r0, c0, c0 & ~3, H, acc);
+    tile_store<CT>(X + o * TLD + o + H, r0, c0, acc);
+  } else {
+    // T = U_AB Uinv_BB -> X_AB slot
+    tile_mm<CT>(S + (o + H) * TLD + o, X + (o + H) * TLD + o + H, r0, c0, 0, (c0 + CT + 3) & ~3, acc);
+    tile_store<CT>(X + (o + H) * TLD + o, r0, c0, acc);
+  }
+  half_sync(bar);
+  float acc2[4][CT] = {};
+  if (!UPPER) {
+    // X_BA = -Linv_BB T
+    tile_mm<CT>(X + (o + H) * TLD + o + H, X + o * TLD + o + H, r0, c0, 0, r0 + 4, acc2);
+  } else {
+    // X_AB = -Uinv_AA T
+    tile_mm<CT>(X + o * TLD + o, X + (o + H) * TLD + o, r0, c0, r0, H, acc2);
+  }
+  half_sync(bar);
+  if (!UPPER) tile_store_neg<CT>(X + o * TLD + o + H, r0, c0, acc2);
+  else tile_store_neg<CT>(X + (o + H) * TLD + o, r0, c0, acc2);
+  half_sync(bar);
+}
+
+__global__ void __launch_bounds__(512) k_diag_tiled(float* __restrict__ A, int64_t ld, int k,
+                                                    float* __restrict__ Dinv, int* __restrict__ info) {
+  extern __shared__ __align__(16) float dsm[];
+  float* S = dsm;                 // A -> L\U
+  float* Li = S + LU_NB * TLD;    // L^{-1}
+  float* Ui = Li + LU_NB * TLD;   // U^{-1}
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const size_t off = (size_t)k * LU_NB;
+  float* Ab = A + off + off * ld;
+  {
+    // 8 float4 per thread, all loads in flight before the first store
+    float4 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
+      v[i] = __ldcg((const float4*)(Ab + r4 + (size_t)c * ld));
+    }
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
+      *(float4*)&S[c * TLD + r4] = v[i];
+      *(float4*)&Li[c * TLD + r4] = z;
+      *(float4*)&Ui[c * TLD + r4] = z;
+    }
+  }
+  __syncthreads();
+  int bad = 0;
+  for (int p = 0; p < LU_NB / DB; ++p) {
+    const int jb = p * DB;
+    // F1
+    if (warp == 0) {
+      float P[4][DB];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int r = jb + lane + 32 * m;
+#pragma unroll
+        for (int c = 0; c < DB; ++c) P[m][c] = (r < LU_NB) ? S[(jb + c) * TLD + r] : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < DB; ++c) {
+        const float piv = __shfl_sync(0xffffffffu, P[0][c], c);
+        if (!(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
+        const float inv = 1.f / piv;
+        float uu[DB];
+#pragma unroll
+        for (int c2 = c + 1; c2 < DB; ++c2) uu[c2] = __shfl_sync(0xffffffffu, P[0][c2], c);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          if (lane + 32 * m > c && jb + lane + 32 * m < LU_NB) {
+            const float l = P[m][c] * inv;
+            P[m][c] = l;
+#pragma unroll
+            for (int c2 = c + 1; c2 < DB; ++c2) P[m][c2] -= l * uu[c2];
+          }
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int r = jb + lane + 32 * m;
+        if (r < LU_NB) {
+#pragma unroll
+          for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + r] = P[m][c];
+        }
+      }
+      // inverse of the 16 x 16 unit-lower block: lane r owns row r
+      float X[DB];
+#pragma unroll
+      for (int c = 0; c < DB; ++c) X[c] = (lane == c) ? 1.f : 0.f;
+#pragma unroll
+      for (int q = 0; q < DB - 1; ++q) {
+        const float l = P[0][q];
+#pragma unroll
+        for (int c = 0; c <= q; ++c) {
+          const float xq = __shfl_sync(0xffffffffu, X[c], q);
+          if (lane > q && lane < DB) X[c] -= l * xq;
+        }
+      }
+      if (lane < DB) {
+#pragma unroll
+        for (int c = 0; c < DB; ++c) Li[(jb + c) * TLD + jb + lane] = X[c];
+      }
+    }
+    __syncthreads();
+    if (jb + DB == LU_NB) break;
+    // F2: U block row, one thread per column
+    for (int c = jb + DB + t; c < LU_NB; c += 512) {
+      float v[DB], o[DB];
+#pragma unroll
+      for (int q4 = 0; q4 < DB; q4 += 4) {
+        const float4 a = *(const float4*)&S[c * TLD + jb + q4];
+        v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
+      }
+#pragma unroll
+      for (int i = 0; i < DB; ++i) o[i] = 0.f;
+#pragma unroll
+      for (int q = 0; q < DB; ++q) {
+#pragma unroll
+        for (int i4 = 0; i4 < DB; i4 += 4) {
+          const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
+          o[i4] = fmaf(l.x, v[q], o[i4]);
+          o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
+          o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
+          o[i4 + 3] = fmaf(l.w, v[q], o[i4 + 3]);
+        }
+      }
+#pragma unroll
+      for (int q4 = 0; q4 < DB; q4 += 4)
+        *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
+    }
+    __syncthreads();
+    // F3: trailing update on 4 x 4 tiles
+    {
+      const int n = LU_NB - jb - DB, nt = n / 4;
+      const float* Pb = S + jb * TLD + jb + DB;       // L21(r, q)
+      const float* Qb = S + (jb + DB) * TLD + jb;     // U12(q, c)
+      float* Cb = S + (jb + DB) * TLD + jb + DB;
+      for (int idx = t; idx < nt * nt; idx += 512) {
+        const int r0 = 4 * (idx % nt), c0 = 4 * (idx / nt);
+        float acc[4][4] = {};
+        tile_mm<4>(Pb, Qb, r0, c0, 0, DB, acc);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float4 cv = *(float4*)&Cb[(c0 + j) * TLD + r0];
+          cv.x -= acc[0][j]; cv.y -= acc[1][j]; cv.z -= acc[2][j]; cv.w -= acc[3][j];
+          *(float4*)&Cb[(c0 + j) * TLD + r0] = cv;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (bad) atomicExch(info, k + 1);
+  if (warp < 8) {
+    // L^{-1}: its 16 x 16 diagonal inverses are in place
+    const int u = t;
+    inv_level<16, false>(S, Li, u, 1);
+    inv_level<32, false>(S, Li, u, 1);
+    inv_level<64, false>(S, Li, u, 1);
+  } else {
+    // U^{-1}: warp 8 + w inverts the 16 x 16 diagonal block w (lane = row)
+    {
+      const int jb = (warp - 8) * DB;
+      float urow[DB], acc[DB];
+#pragma unroll
+      for (int c = 0; c < DB; ++c) {
+        urow[c] = (lane < DB) ? S[(jb + c) * TLD + jb + lane] : 0.f;
+        acc[c] = 0.f;
+      }
+#pragma unroll
+      for (int q = DB - 1; q >= 0; --q) {
+        const float uqq = __shfl_sync(0xffffffffu, urow[q], q);
+        const float inv = 1.f / uqq;
+#pragma unroll
+        for (int c = 0; c < DB; ++c) {
+          float x = (c >= q) ? (((c == q) ? 1.f : 0.f) + acc[c]) * inv : 0.f;
+          x = __shfl_sync(0xffffffffu, x, q);
+          if (lane == q) acc[c] = x;
+          else if (lane < q) acc[c] -= urow[q] * x;
+        }
+      }
+      if (lane < DB) {
+#pragma unroll
+        for (int c = 0; c < DB; ++c) Ui[(jb + c) * TLD + jb + lane] = acc[c];
+      }
+    }
+    half_sync(2);
+    const int u = t - 256;
+    inv_level<16, true>(S, Ui, u, 2);
+    inv_level<32, true>(S, Ui, u, 2);
+    inv_level<64, true>(S, Ui, u, 2);
+  }
+  __syncthreads();
+  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  float* Uo = Lo + LU_NB * LU_NB;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
+    *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&S[c * TLD + r4];
+    *(float4*)(Lo + r4 + c * LU_NB) = *(const float4*)&Li[c * TLD + r4];
+    *(float4*)(Uo + r4 + c * LU_NB) = *(const float4*)&Ui[c * TLD + r4];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Panels of one LU step in FP32 (CUDA cores): U12 = Linv A12 and
+// L21 = A21 Uinv, in place.  A CTA owns all 128 rows (U panel) or all 128
+// columns (L panel) of its 32-wide slice, so it reads its whole slice before
+// writing it back and slices never overlap.
+// ---------------------------------------------------------------------------
+constexpr int PW = 32;  // slice width
+constexpr int PANEL_SMEM = sizeof(float) * (LU_NB * TLD + LU_NB * (PW + 4));
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+// blockIdx.y == 0: U panel, columns [32 x, 32 x + 32) of B (128 rows, ld)
+//   <- Linv B; thread tile rows 4 (t & 31) .. +3, columns 4 (t >> 5) .. +3.
+// blockIdx.y == 1: L panel, rows [32 x, 32 x + 32) of Ap (128 columns, ld)
+//   <- Ap Uinv; thread tile rows 4 (t >> 5) .. +3, columns (t & 31) + 32 j,
+//   written back through shared memory so that the stores coalesce.
+__global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Linv, float* B,
+                                                const float* __restrict__ Uinv, float* Ap, int64_t ld) {
+  extern __shared__ __align__(16) float psm[];
+  float* Ms = psm;                   // Linv or Uinv, column-major, ld TLD
+  float* Xs = psm + LU_NB * TLD;     // the slice
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (blockIdx.y == 0) {
+    float* Bb = B + (size_t)blockIdx.x * PW * ld;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int idx = t + 256 * i, r4 = 4 * (idx & 31), kx = idx >> 5;
+      cp_async16(&Ms[kx * TLD + r4], Linv + r4 + kx * LU_NB);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = t + 256 * i, k4 = 4 * (idx & 31), c = idx >> 5;
+      cp_async16(&Xs[c * TLD + k4], Bb + k4 + (size_t)c * ld);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int r0 = 4 * lane, c0 = 4 * warp;
+    float acc[4][4] = {};
+    tile_mm<4>(Ms, Xs, r0, c0, 0, LU_NB, acc);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      *(float4*)&Bb[r0 + (size_t)(c0 + j) * ld] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+  } else {
+    float* Ab = Ap + (size_t)blockIdx.x * PW;
+    constexpr int XLD = PW + 4;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int idx = t + 256 * i, k4 = 4 * (idx & 31), c = idx >> 5;
+      cp_async16(&Ms[c * TLD + k4], Uinv + k4 + c * LU_NB);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = t + 256 * i, r4 = 4 * (idx & 7), kx = idx >> 3;
+      cp_async16(&Xs[kx * XLD + r4], Ab + r4 + (size_t)kx * ld);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int r0 = 4 * warp;
+    float acc[4][4] = {};
+    for (int q = 0; q < LU_NB; q += 4) {
+      float4 p[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) p[i] = *(const float4*)&Xs[(q + i) * XLD + r0];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float4 qv = *(const float4*)&Ms[(lane + 32 * j) * TLD + q];
+        const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          acc[0][j] = fmaf(p[i].x, qq[i], acc[0][j]);
+          acc[1][j] = fmaf(p[i].y, qq[i], acc[1][j]);
+          acc[2][j] = fmaf(p[i].z, qq[i], acc[2][j]);
+          acc[3][j] = fmaf(p[i].w, qq[i], acc[3][j]);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      *(float4*)&Xs[(lane + 32 * j) * XLD + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = t + 256 * i, r4 = 4 * (idx & 7), c = idx >> 3;
+      *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&Xs[c * XLD + r4];
+    }
+  }
+}
+
 static void lu_attrs() {
   static bool attr = false;
   if (attr) return;
   attr = true;
-  cudaFuncSetAttribute(k_diag_factor, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(sizeof(float) * 3 * LU_NB * DLD));
   cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float) * LU_NB * DLD));
+  cudaFuncSetAttribute(k_diag_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(sizeof(float) * 3 * LU_NB * TLD));
   cudaFuncSetAttribute(k_gemm_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
   cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
+  cudaFuncSetAttribute(k_panels, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM);
 }
 
 // diagonal block k and its two panels: U12 = Linv A12, L21 = A21 Uinv
@@ -694,15 +992,16 @@ static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* in
                             cudaStream_t st) {
   const size_t kk = (size_t)k * LU_NB;
   const int rem = Npad - (int)kk - LU_NB;
-  k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A, ld, k, Dinv, info);
+  k_diag_tiled<<<1, 512, sizeof(float) * 3 * LU_NB * TLD, st>>>(A, ld, k, Dinv, info);
   count_launches(1);
   if (rem <= 0) return;
   const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
   const float* Ui = Li + LU_NB * LU_NB;
   float* A12 = A + kk + (kk + LU_NB) * ld;
   float* A21 = A + (kk + LU_NB) + kk * ld;
-  gemm_tile128(Li, LU_NB, A12, ld, A12, ld, LU_NB, rem, 1.f, 0.f, x3, st);
-  gemm_tile128(A21, ld, Ui, LU_NB, A21, ld, rem, LU_NB, 1.f, 0.f, x3, st);
+  (void)x3;  // panels in full FP32 on the CUDA cores
+  k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(Li, A12, Ui, A21, ld);
+  count_launches(1);
 }
 
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
@@ -890,4 +1189,16 @@ void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStre
   k_from_f32_scale<<<(N + 255) / 256, 256, 0, st>>>(y, cs, N, z);
 }
 
+}  // namespace bem
+
+namespace bem {
+// Self-check: factor the diagonal block at (0, 0) of A1 with the blocked
+// kernel and of A2 (a copy) with the register-blocked Gauss-Jordan kernel;
+// D1, D2 receive the two pairs of triangular inverses.
+void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, int* info, cudaStream_t st) {
+  lu_attrs();
+  k_diag_tiled<<<1, 512, sizeof(float) * 3 * LU_NB * TLD, st>>>(A1, ld, 0, D1, info);
+  k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
+  count_launches(2);
+}
 }  // namespace bem

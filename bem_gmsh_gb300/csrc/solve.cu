@@ -440,9 +440,31 @@ __global__ void k_maxdiff(const float* A, const float* B, int64_t cnt, float* ou
 // with the legacy mma.sync ones; out[0] = max |difference of the factors|,
 // out[1] = max |factor|, out[2] / out[3] = factor times (ms) tcgen05 / legacy.
 extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
-  if (!c || !out || which != 1 || n < LU_NB || n % LU_NB != 0 || n > 16384) return BEM_ERR_INVALID;
+  if (!c || !out || (which != 1 && which != 2) || n < LU_NB || n % LU_NB != 0 || n > 16384)
+    return BEM_ERR_INVALID;
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
+  if (which == 2) {
+    float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
+    float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);
+    float* D = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * 4 * LU_NB * LU_NB);
+    int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
+    if (!A1 || !A2 || !D || !info) return BEM_ERR_NOMEM;
+    k_fill_test<<<1024, 256, 0, st>>>(A1, n, n, 777u);
+    cudaMemcpyAsync(A2, A1, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(info, 0, 16, st);
+    bem::diag_selftest(A1, A2, n, D, D + 2 * LU_NB * LU_NB, info, st);
+    float* d = (float*)(info + 8);
+    float h[6];
+    cudaMemsetAsync(d, 0, 24, st);
+    k_maxdiff<<<512, 256, 0, st>>>(A1, A2, (int64_t)n * LU_NB, d);  // first block column
+    k_maxdiff<<<512, 256, 0, st>>>(D, D + 2 * LU_NB * LU_NB, 2 * LU_NB * LU_NB, d + 2);
+    cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "selftest diag");
+    out[0] = h[0]; out[1] = h[1]; out[2] = h[2]; out[3] = h[3];
+    return BEM_OK;
+  }
   const int K = n / LU_NB;
   float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
   float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);

@@ -28,6 +28,8 @@ def test_solve_system_dense(n, mode):
     x, st = solve_system(A, b, mode=mode)
     xr = np.linalg.solve(A, b)
     assert rel(x, xr) < 1e-12, (rel(x, xr), st)
+    if mode == "mixed":  # an FP32-accurate LU preconditioner needs only a few iterations
+        assert st["iterations"] <= 8, st
 
 
 def test_solve_system_device_pointers():
@@ -82,6 +84,7 @@ def test_star_pipeline_mixed(orc, ne):
     scale = np.linalg.norm(ref.cache["x"]) / np.linalg.norm(analytical(ref))
     assert abs(rel_error(dad) - rel_error(ref)) <= bar * scale + 1e-12
     assert st["rel_residual"] <= 1e-14
+    assert st["iterations"] <= 8, st
 
 
 def test_kelvin_patch_pipeline(orc):
@@ -105,3 +108,14 @@ def test_solve_bad_args():
     A = np.asfortranarray(np.eye(4))
     with pytest.raises(BemError):
         solve_system(A, np.ones(4), tol=-1.0)
+
+
+def test_lu_building_blocks():
+    """The tensor-core trailing updates and the blocked diagonal factorization
+    agree with the independent implementations to FP32 rounding."""
+    from bem_gmsh_gb300 import _lib
+    c = _lib.default_context()
+    d = c.selftest_diag(256)
+    assert d[0] / d[1] < 1e-5 and d[2] / d[3] < 1e-5, d
+    r = c.selftest_lu(1024)
+    assert r[0] / r[1] < 1e-5, r
