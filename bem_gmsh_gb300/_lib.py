@@ -16,6 +16,7 @@ BEM_MEM_HOST, BEM_MEM_DEVICE = 0, 1
 BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
 BEM_OPT_TCGEN05 = 1
 BEM_OPT_KERNEL_TIMING = 2
+BEM_OPT_FAR_DF = 3
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total"]
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",

@@ -23,6 +23,7 @@
 #include "bem_device.cuh"
 #include "bem_kernels.h"
 #include "bem_prof.h"
+#include "df32.cuh"
 
 namespace bem {
 
@@ -63,6 +64,38 @@ __global__ void pack_nodes_kernel(GeomDev g, Rules R, Physics ph, NodeRec* nodes
     r.cG = (float)wjk;
     r.cH = (float)wjk;
   }
+  nodes[j] = r;
+}
+
+// double-float log table (one thread per entry)
+__global__ void logtab_kernel(float4* t) {
+  const int i = threadIdx.x;
+  if (i < df::kLogTable) {
+    const df::LogEntry e = df::log_entry(i);
+    t[i] = make_float4(e.rc_h, e.rc_l, e.lc_h, e.lc_l);
+  }
+}
+
+// double-float node record (Laplace): G = log(R2) cG, H = (r.n) / R2 cH with
+// the constants of laplace_UT times J w, and the boundary value of the node
+__global__ void pack_nodes_df_kernel(GeomDev g, Rules R, Physics ph, const double* bv, NodeDF* nodes) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.n) return;
+  NodeDF r;
+  df::split3(g.px[j], r.xa, r.xb, r.xc);
+  df::split3(g.py[j], r.ya, r.yb, r.yc);
+  df::f2 t = df::from_double(g.nx[j]);
+  r.nxh = t.h; r.nxl = t.l;
+  t = df::from_double(g.ny[j]);
+  r.nyh = t.h; r.nyl = t.l;
+  const double wjk = g.jac[j] * R.ew[j % g.nn];
+  const double inv2pi = 1.0 / (2 * kPi);
+  t = df::from_double(-(0.5 * inv2pi / ph.k) * wjk);
+  r.cGh = t.h; r.cGl = t.l;
+  t = df::from_double(inv2pi * wjk);
+  r.cHh = t.h; r.cHl = t.l;
+  t = df::from_double(bv ? bv[j] : 0.0);
+  r.bvh = t.h; r.bvl = t.l;
   nodes[j] = r;
 }
 
@@ -207,9 +240,13 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
   constexpr int BE = 32;                   // elements per tile
   const int nn = a.nn;
 
+  constexpr int NDB = (PREC == 3) ? (int)sizeof(NodeDF) : (int)sizeof(NodeRec);
   __shared__ __align__(16) ElemRec s_el[BE];
-  __shared__ __align__(16) NodeRec s_nd[BE * BEM_MAXNN];
+  __shared__ __align__(16) unsigned char s_ndraw[BE * BEM_MAXNN * NDB];
+  __shared__ __align__(16) float4 s_log[PREC == 3 ? df::kLogTable : 1];
   __shared__ __align__(8) uint64_t s_bar;
+  const NodeRec* s_nd = (const NodeRec*)s_ndraw;
+  const NodeDF* s_ndf = (const NodeDF*)s_ndraw;
   __shared__ double s_red[EL][32 * SPT * DOF * DOF];
   __shared__ double s_redb[EL][32 * SPT * DOF];
 
@@ -225,13 +262,19 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
     mbar_init(&s_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  if constexpr (PREC == 3) {
+    for (int i = tid; i < df::kLogTable; i += blockDim.x) s_log[i] = a.logtab[i];
+  }
   __syncthreads();
   if (tid == 0) {
     uint32_t eb = (uint32_t)(ne_t * sizeof(ElemRec));
-    uint32_t nb = (uint32_t)(ne_t * nn * sizeof(NodeRec));
+    uint32_t nb = (uint32_t)(ne_t * nn * NDB);
     mbar_expect_tx(&s_bar, eb + nb);
     bulk_g2s(s_el, a.elems + e0, eb, &s_bar);
-    bulk_g2s(s_nd, a.nodes + (size_t)e0 * nn, nb, &s_bar);
+    if constexpr (PREC == 3)
+      bulk_g2s(s_ndraw, a.nodes_df + (size_t)e0 * nn, nb, &s_bar);
+    else
+      bulk_g2s(s_ndraw, a.nodes + (size_t)e0 * nn, nb, &s_bar);
   }
   // block-uniform decision: either every thread saw the copy land or the
   // whole CTA reports the timeout and leaves
@@ -255,6 +298,18 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
     if constexpr (PREC != 0) {
       sx[s] = a.px[ic];
       sy[s] = a.py[ic];
+    }
+  }
+  // double-float state: three-float source coordinates, row sums and b
+  float s3x[PREC == 3 ? SPT : 1][3], s3y[PREC == 3 ? SPT : 1][3];
+  df::f2 rs_df[PREC == 3 ? SPT : 1], b_df[PREC == 3 ? SPT : 1];
+  if constexpr (PREC == 3) {
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+      df::split3(sx[s], s3x[s][0], s3x[s][1], s3x[s][2]);
+      df::split3(sy[s], s3y[s][0], s3y[s][1], s3y[s][2]);
+      rs_df[s] = df::f2{0.f, 0.f};
+      b_df[s] = df::f2{0.f, 0.f};
     }
   }
 
@@ -294,6 +349,43 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
           if (slot < a.pair_cap) a.pairs[slot] = make_int2(src0 + s, e);
         }
       }
+    }
+    if constexpr (PREC == 3) {
+      static_assert(NC == 1 && FUSED, "double-float far field: fused Laplace only");
+      const df::LogEntry* tab = (const df::LogEntry*)s_log;
+      for (int k = 0; k < nn; ++k) {
+        const NodeDF nd = s_ndf[el * nn + k];
+        const int j = e * nn + k;
+        const bool gcol = a.bc[j] == 0;  // column takes -G and b takes -H bv
+        const df::f2 cG{nd.cGh, nd.cGl}, cH{nd.cHh, nd.cHl};
+        const df::f2 nxd{nd.nxh, nd.nxl}, nyd{nd.nyh, nd.nyl};
+        const df::f2 bvv = gcol ? df::f2{-nd.bvh, -nd.bvl} : df::f2{nd.bvh, nd.bvl};
+        double av[SPT];
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) {
+          df::f2 Hs{0.f, 0.f}, Gs{0.f, 0.f};
+          if (far[s]) {
+            const df::f2 rx = df::diff3(nd.xa, nd.xb, nd.xc, s3x[s][0], s3x[s][1], s3x[s][2]);
+            const df::f2 ry = df::diff3(nd.ya, nd.yb, nd.yc, s3y[s][0], s3y[s][1], s3y[s][2]);
+            const df::f2 R2 = df::add(df::sqr(rx), df::sqr(ry));
+            Gs = df::mul(df::log(R2, tab), cG);
+            const df::f2 num = df::add(df::mul(rx, nxd), df::mul(ry, nyd));
+            Hs = df::mul(df::div(num, R2), cH);
+          }
+          rs_df[s] = df::add(rs_df[s], Hs);
+          b_df[s] = df::add(b_df[s], df::mul(gcol ? Hs : Gs, bvv));
+          av[s] = df::to_double(gcol ? df::neg(Gs) : Hs);
+        }
+        double* Ac = (double*)a.H + (size_t)src0 + (size_t)j * ld;
+        if (vec_ok) {
+          *(double2*)Ac = make_double2(av[0], av[1]);
+        } else {
+#pragma unroll
+          for (int s = 0; s < SPT; ++s)
+            if (src0 + s < a.nt) Ac[s] = av[s];
+        }
+      }
+      continue;
     }
     for (int k = 0; k < nn; ++k) {
       const NodeRec nd = s_nd[el * nn + k];
@@ -390,6 +482,13 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
       }
     }
   }
+  if constexpr (PREC == 3) {
+#pragma unroll
+    for (int s = 0; s < SPT; ++s) {
+      rowsum[s][0] = (double)rs_df[s].h + (double)rs_df[s].l;
+      bacc[s] = (double)b_df[s].h + (double)b_df[s].l;
+    }
+  }
   // reduce row sums across element lanes, one FP64 atomic per row
 #pragma unroll
   for (int r = 0; r < SPT * DOF; ++r) {
@@ -439,6 +538,12 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fa.pair_cap = q.pair_cap;
   fa.ph = q.ph;
   fa.rows = q.rows; fa.nodes = q.nodes; fa.elems = q.elems;
+  fa.nodes_df = q.nodes_df; fa.logtab = q.logtab;
+  if constexpr (PREC == 3) {
+    logtab_kernel<<<1, 160, 0, st>>>(q.logtab);
+    pack_nodes_df_kernel<<<(g.n + 255) / 256, 256, 0, st>>>(g, q.R, q.ph, q.bv, q.nodes_df);
+    count_launches(2);
+  }
   fa.px = g.px; fa.py = g.py; fa.nx = g.nx; fa.ny = g.ny; fa.jac = g.jac;
   for (int k = 0; k < BEM_MAXNN; ++k) fa.ew[k] = q.R.ew[k];
   fa.H = q.H; fa.G = q.G; fa.A32 = q.A32;
@@ -460,7 +565,7 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   na.pair_count = q.counters; na.pairs = q.pairs;
   na.H = q.H; na.G = q.G; na.A32 = q.A32;
   na.bc = q.bc; na.bv = q.bv; na.b = q.b; na.rowsum = q.rowsum; na.gdiag = q.gdiag;
-  na.mode = PREC == 0 ? 0 : (!FUSED ? 1 : (MIXED ? 3 : 2));
+  na.mode = PREC == 0 ? 0 : (!FUSED ? 1 : (MIXED ? 3 : 2));  // PREC 3: fused FP64 (2)
 
   FinalArgs fi{};
   fi.nt = g.nt; fi.n = g.n; fi.ld = q.ld; fi.H = q.H; fi.A32 = q.A32;
@@ -499,6 +604,7 @@ int launch_assembly(const AsmRequest& q, cudaStream_t st) {
     case 10: launch_variant<1, 1, false>(q, st); break;
     case 11: launch_variant<1, 1, true>(q, st); break;
     case 21: launch_variant<1, 2, true>(q, st); break;
+    case 31: launch_variant<1, 3, true>(q, st); break;
     case 100: launch_variant<4, 0, false>(q, st); break;
     case 110: launch_variant<4, 1, false>(q, st); break;
     case 111: launch_variant<4, 1, true>(q, st); break;

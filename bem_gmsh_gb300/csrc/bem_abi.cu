@@ -288,6 +288,11 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
   q.counters = (int*)c->get(bem_ctx::SLOT_COUNTERS, 64);
   q.absmax = (unsigned long long*)((char*)q.counters + 32);
   if (!q.rows || !q.nodes || !q.elems || !q.rowsum || !q.gdiag || !q.counters) return BEM_ERR_NOMEM;
+  if (q.prec == 3) {
+    q.nodes_df = (bem::NodeDF*)c->get(bem_ctx::SLOT_NODES_DF, sizeof(bem::NodeDF) * (size_t)q.g.n);
+    q.logtab = (float4*)c->get(bem_ctx::SLOT_LOGTAB, sizeof(float4) * 136);
+    if (!q.nodes_df || !q.logtab) return BEM_ERR_NOMEM;
+  }
   int cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : nt * 16 + 4096;
   for (int attempt = 0; attempt < 3; ++attempt) {
     q.pairs = (int2*)c->get(bem_ctx::SLOT_PAIRS, sizeof(int2) * (size_t)cap);
@@ -437,13 +442,14 @@ extern "C" int bem_assemble_system2d(bem_ctx* c, const bem_geom2d* g, int kind, 
   const int dof = kind == 0 ? 1 : 2;
   const int64_t rows = (int64_t)dof * g->nt;
   if (lda < rows) return BEM_ERR_INVALID;
+  const int prec = (kind == 0 && c->opt_far_df >= 2) ? 3 : 1;
   if (mem == BEM_MEM_DEVICE)
-    return bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, 1, A, lda, nullptr, b);
+    return bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, prec, A, lda, nullptr, b);
   const int64_t ldp = (rows + 3) / 4 * 4;
   double* dA = (double*)c->get(bem_ctx::SLOT_OUT0, sizeof(double) * (size_t)ldp * rows);
   double* db = (double*)c->get(bem_ctx::SLOT_OUT1, sizeof(double) * (size_t)rows);
   if (!dA || !db) return BEM_ERR_NOMEM;
-  int rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, 1, dA, ldp, nullptr, db);
+  int rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, prec, dA, ldp, nullptr, db);
   if (rc) return rc;
   cudaMemcpy2DAsync(A, 8 * lda, dA, 8 * ldp, 8 * rows, rows, cudaMemcpyDeviceToHost, c->stream);
   cudaMemcpyAsync(b, db, 8 * rows, cudaMemcpyDeviceToHost, c->stream);

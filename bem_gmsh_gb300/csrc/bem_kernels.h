@@ -14,6 +14,16 @@ struct __align__(16) NodeRec {
   float cG, cH;          // folded kernel constants times J w
 };
 
+// 64-byte node record of the double-float far field (Laplace): coordinates
+// as exact three-float splits, normal, kernel constants and boundary value
+// as hi + lo pairs (G = log(R2) cG, H = (r.n) / R2 cH).
+struct __align__(16) NodeDF {
+  float xa, xb, xc, ya, yb, yc;
+  float nxh, nxl, nyh, nyl;
+  float cGh, cGl, cHh, cHl;
+  float bvh, bvl;
+};
+
 // 32-byte element record: conservative bounding box + squared near limit.
 struct __align__(16) ElemRec {
   float lox, loy, hix, hiy;
@@ -27,6 +37,8 @@ struct FarArgs {
   Physics ph;
   const float4* rows;
   const NodeRec* nodes;
+  const NodeDF* nodes_df;   // double-float variant only
+  const float4* logtab;     // double-float log table (129 entries)
   const ElemRec* elems;
   const double *px, *py, *nx, *ny, *jac;
   double ew[BEM_MAXNN];
@@ -83,7 +95,8 @@ struct AsmRequest {
   Rules R;
   Physics ph;
   double near_factor;
-  int prec;    // 0 FP32, 1 FP64, 2 FP64 + FP32 copy of A
+  int prec;    // 0 FP32, 1 FP64, 2 FP64 + FP32 copy of A, 3 FP64 output with the
+               // far field in double-float (Laplace, fused)
   int fused;   // 1: write A, b (applyBC fused), else H, G
   void* H;
   int64_t ld;
@@ -96,6 +109,8 @@ struct AsmRequest {
   // workspace
   float4* rows;
   NodeRec* nodes;
+  NodeDF* nodes_df;
+  float4* logtab;
   ElemRec* elems;
   double* rowsum;
   double* gdiag;

@@ -373,7 +373,9 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   double* dx = mem == BEM_MEM_DEVICE ? x : bx + N;
   Timer ta;
   ta.start(c->stream);
-  rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, 1, A, ld, nullptr, b);
+  // the FP64 comparison path keeps FP64 arithmetic throughout
+  const int prec = (mode == BEM_SOLVE_MIXED && kind == 0 && c->opt_far_df >= 1) ? 3 : 1;
+  rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, prec, A, ld, nullptr, b);
   ta.stop(c->stream);
   if (rc) return rc;
   double t_asm = ta.ms();
@@ -400,6 +402,11 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   }
   if (option == BEM_OPT_KERNEL_TIMING) {
     c->prof.on = value != 0;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_FAR_DF) {
+    if (value < 0 || value > 2) return BEM_ERR_INVALID;
+    c->opt_far_df = value;
     return BEM_OK;
   }
   return BEM_ERR_INVALID;

@@ -269,37 +269,45 @@ def main():
                                  e2e_dad.geo, e2e_dad.elem_weight, e2e_dad.BC, e2e_dad.BV))
     d2h = 8 * N
 
-    # roofline of the dominant kernel class (device time over the timed region)
+    # roofline of every kernel class over the timed region, and of the dominant one.
+    # achieved = algorithmic units of one solve x steps / device time of the class.
     hbm, bf16, src = peaks()
     nb = (N + 127) // 128 * 128
+    rems = [nb - (k + 1) * 128 for k in range(nb // 128)]
+    iters_last = max(1, iters[-1] if iters else 1)
     algo = {
-        # bytes: the FP64 system matrix written once per assembly
-        "far": ("hbm", 8.0 * N * N, "GB/s"),
-        # bytes: FP64 A read + FP32 A written
-        "lu_prep": ("hbm", 12.0 * N * N, "GB/s"),
-        # flops: 2 (rem-128)^2 128 per step, summed over the factorization
-        "lu_trail": ("tensor", sum(2.0 * (nb - (k + 2) * 128) ** 2 * 128 for k in range(nb // 128 - 1)),
-                     "TFLOP/s"),
-        # bytes: one FP64 matrix read per product
-        "gemv": ("hbm", 8.0 * N * N, "GB/s"),
+        # bytes: the FP64 system matrix A written once
+        "far": ("hbm", 8.0 * N * N, "GB/s", "FP64 A written, 8 B/entry"),
+        # bytes: 8 B/pair of listed near pairs is negligible; FP64 issue bound
+        "near": ("hbm", 8.0 * 24 * N, "GB/s", "near/singular entries, FP64 issue bound"),
+        # bytes: FP64 A read twice (column scales, conversion) + FP32 copy written
+        "lu_prep": ("hbm", 16.0 * N * N + 4.0 * nb * nb, "GB/s", "A64 read x2 + A32 written"),
+        # flops: diagonal block (4/3 128^3) + both panels (4 128^2 rem) + the
+        # look-ahead column and row block updates (4 128^2 rem) per step
+        "lu_crit": ("tensor", sum(4.0 / 3.0 * 128 ** 3 + 8.0 * 128 * 128 * r for r in rems), "TFLOP/s",
+                    "latency-bound chain: one diagonal block per step on one SM"),
+        # flops: bulk trailing updates, 2 rem'^2 128 per step (3xTF32 counts once)
+        "lu_trail": ("tensor", sum(2.0 * max(r - 128, 0) ** 2 * 128 for r in rems), "TFLOP/s",
+                     "3xTF32 tcgen05 trailing updates"),
+        # bytes: FP32 L and U read once per preconditioner application
+        "trsv": ("hbm", 4.0 * nb * nb * iters_last, "GB/s", "FP32 LU read per sweep pair"),
+        # bytes: one FP64 A read per product (initial residual + one per iteration + final)
+        "gemv": ("hbm", 8.0 * N * N * (iters_last + 2), "GB/s", "FP64 A read per product"),
     }
-    shares = {k: v[0] for k, v in ktimes.items() if k != "lu_total"}
-    dom = max((k for k in shares if k in algo), key=lambda k: shares[k])
-    bound, units_total, unit = algo[dom]
-    groups = max(1, ktimes[dom][1])
-    # per launch group: far/lu_prep once per solve, lu_trail = all steps of one LU, gemv per product
-    per_solve = {"far": 1, "lu_prep": 1, "lu_trail": None, "gemv": None}[dom]
-    t_avg_s = ktimes[dom][0] / groups * 1e-3
-    if dom == "lu_trail":
-        units = units_total / (nb // 128 - 1)  # average per step group
-    else:
-        units = units_total
-    achieved = units / t_avg_s / (1e9 if bound == "hbm" else 1e12)
-    peak = hbm if bound == "hbm" else bf16
-    roof = {"kernel_class": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "traffic": None, "peak_source": src,
-            "note": ("tensor peak is the measured dense bf16 burst; the TF32 dense rate is half of it"
-                     if bound == "tensor" else "measured copy bandwidth")}
+    classes = {}
+    for k, (bound, units, unit, note) in algo.items():
+        ms_k = ktimes.get(k, (0.0, 0))[0]
+        if ms_k <= 0:
+            continue
+        ach = units * args.steps / (ms_k * 1e-3) / (1e9 if bound == "hbm" else 1e12)
+        pk = hbm if bound == "hbm" else bf16
+        classes[k] = {"bound": bound, "achieved": ach, "unit": unit, "peak": pk, "frac": ach / pk,
+                      "ms_per_step": ms_k / args.steps, "note": note}
+    dom = max(classes, key=lambda k: classes[k]["ms_per_step"])
+    roof = dict(classes[dom])
+    roof.update({"kernel_class": dom, "traffic": None, "peak_source": src,
+                 "peak_note": ("measured dense bf16 burst (TF32 dense is half of it)"
+                               if roof["bound"] == "tensor" else "measured copy bandwidth")})
 
     # CPU baseline: the oracle port on the host cores, one full solve sample
     cpu_ts, x_orc = cpu_reference(make, max(1, args.cpu_samples), 0, args.npg)
@@ -324,7 +332,7 @@ def main():
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()},
             "e2e": {"value": 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": roof,
+            "roofline": roof, "roofline_classes": classes,
             "cpu_baseline": {"value": cpu_v, "unit": "solves/s", "cores": cores, "kind": "port",
                              "sample": f"{len(cpu_ts)} full solve(s) of the same workload: oracle assembly on "
                                        f"{cores} threads + LAPACK LU"},

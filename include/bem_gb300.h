@@ -47,6 +47,9 @@ extern "C" {
 /* context options (bem_ctx_set_option) */
 #define BEM_OPT_TCGEN05 1       /* 1 (default): LU trailing updates on tcgen05; 0: legacy mma.sync */
 #define BEM_OPT_KERNEL_TIMING 2 /* 1: time kernel classes with CUDA events (bem_kernel_times) */
+#define BEM_OPT_FAR_DF 3        /* far-field Laplace entries of FP64 systems evaluated in double-float
+                                   (FP32 pairs, ~1e-14 relative): 0 never, 1 (default) in mixed-precision
+                                   solves, 2 also in bem_assemble_system2d.  Kelvin stays FP64. */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */

@@ -134,6 +134,33 @@ def test_fused_system_matches_applybc(orc, kind):
     assert rel(b, br) < tb, (rel(b, br), tb)
 
 
+@pytest.mark.parametrize("name,mk", [
+    ("star", lambda: star_domain(400, p=2, seed=3, pontointerno=True)),
+    ("quadrado_p2", lambda: quadrado(ndiv=12, ordem=2, pontointerno=True)),
+    ("quadrado_p1", lambda: quadrado(ndiv=30, pontointerno=False)),
+])
+def test_double_float_far_field_matches_fp64(name, mk):
+    """BEM_OPT_FAR_DF = 2: the fused Laplace system with its far field in
+    double-float (FP32 pairs) equals the FP64-arithmetic system to ~1e-14."""
+    from bem_gmsh_gb300 import _lib
+    dad = mk()
+    ctx = _lib.Context()
+    try:
+        ctx.set_option(_lib.BEM_OPT_FAR_DF, 0)
+        A64, b64 = assemble_system(dad, npg=16, ctx=ctx)
+        ctx.set_option(_lib.BEM_OPT_FAR_DF, 2)
+        Adf, bdf = assemble_system(dad, npg=16, ctx=ctx)
+    finally:
+        ctx.close()
+    scale = np.abs(A64).max()
+    d = np.abs(Adf - A64)
+    assert d.max() <= 1e-13 * scale, d.max() / scale
+    # entrywise: within 2^-43 relative (double-float ops are ~2^-48 each)
+    # plus an absolute floor far below the matrix scale
+    assert np.all(d <= 2.0 ** -43 * np.abs(A64) + 1e-16 * scale), float(np.max(d / (np.abs(A64) + 1e-300)))
+    assert np.abs(bdf - b64).max() <= 1e-13 * np.abs(b64).max()
+
+
 def test_device_pointers_and_ld(orc):
     """BEM_MEM_DEVICE with a padded leading dimension."""
     import torch
