@@ -596,29 +596,32 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 }
 
 // ---------------------------------------------------------------------------
-// Tiled factorization of a 128 x 128 diagonal block (no pivoting) and the
+// Factorization of a 128 x 128 diagonal block (no pivoting) with the
 // inverses of its unit-lower and upper triangles, all in shared memory
 // (column-major, ld 132 so that 4 consecutive rows are one 16-byte load).
-//   for each 16-wide panel p (jb = 16 p):
-//     F1  warp 0 factors the (128-jb) x 16 panel in registers (rows over
-//         lanes, pivot rows broadcast by shuffles) and inverts its 16 x 16
-//         unit-lower block;
-//     F2  one thread per column: U[jb:jb+16, c] = Linv_pp A[jb:jb+16, c];
-//     F3  trailing update A22 -= L21 U12 with 4 x 4 register tiles.
-//   then the inverses, L by warps 0-7 and U by warps 8-15 at the same time
-//   (named barriers), by recursive doubling from the 16 x 16 diagonal
-//   inverses: for halves A, B of a 2h block
-//     Linv_BA = -Linv_BB (L_BA Linv_AA),   Uinv_AB = -Uinv_AA (U_AB Uinv_BB),
-//   h = 16, 32, 64, every product on 4 x CT register tiles.
-// 24 block barriers and 9 half-block barriers per half in all.  A and ld
-// must allow 16-byte loads (ld % 4 == 0, 16-byte aligned A).
+// For each 16-wide panel p (jb = 16 p):
+//   A  warps 0-3 factor the panel: every warp holds its own copy of the 16
+//      pivot rows (lane r < 16: row jb + r) and updates them identically, and
+//      32 rows below them (lane: row jb + 16 + 32 w + lane), so no barrier
+//      is needed between columns; the pivot row of each column reaches the
+//      lanes through a double-buffered row in shared memory.  Warp 1 then
+//      inverts the unit-lower 16 x 16 block (one column per lane).
+//      Meanwhile warps 4-15 form the products for the new block row of
+//      L^{-1} and block column of U^{-1}:
+//        T_L = L[p, <p] Linv[<p, <p],   T_U = Uinv[<p, <p] U[<p, p].
+//   B  block row of U: U[p, >p] = Linv_pp A[p, >p]; Linv[p, <p] = -Linv_pp T_L;
+//      warp 12 inverts the upper 16 x 16 block.  Column block p of L\U and
+//      block row p of L^{-1} are final and are written out.
+//   C  Uinv[<p, p] = -T_U Uinv_pp, and the trailing update A22 -= L21 U12 on
+//      4 x 4 register tiles; block column p of U^{-1} is written out.
+// 24 block barriers in all.  A and ld must allow 16-byte accesses
+// (ld % 4 == 0, 16-byte aligned A).
 // ---------------------------------------------------------------------------
-constexpr int DB = 16;        // panel width
-constexpr int TLD = LU_NB + 4;  // shared leading dimension of the tiled kernel
-
-__device__ __forceinline__ void half_sync(int id) {
-  asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory");
-}
+constexpr int DB = 16;          // panel width
+constexpr int TLD = LU_NB + 4;  // shared leading dimension
+// shared floats of the diagonal kernel: L\U, L^{-1}, U^{-1}, four double-
+// buffered pivot rows, the 16 x 16 scratch of the lower inverse
+constexpr int DIAG_SMEM = (int)sizeof(float) * (3 * LU_NB * TLD + 4 * 32 + 16 * 20);
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -646,63 +649,32 @@ __device__ __forceinline__ void tile_mm(const float* Pb, const float* Qb, int r0
 }
 
 template <int CT>
-__device__ __forceinline__ void tile_store_neg(float* Ob, int r0, int c0, const float (&acc)[4][CT]) {
-#pragma unroll
-  for (int j = 0; j < CT; ++j)
-    *(float4*)&Ob[(c0 + j) * TLD + r0] = make_float4(-acc[0][j], -acc[1][j], -acc[2][j], -acc[3][j]);
-}
-
-template <int CT>
 __device__ __forceinline__ void tile_store(float* Ob, int r0, int c0, const float (&acc)[4][CT]) {
 #pragma unroll
   for (int j = 0; j < CT; ++j)
     *(float4*)&Ob[(c0 + j) * TLD + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
 }
 
-// One doubling level of the L (upper = false) or U (upper = true) inverse
-// for half-block size h; u = thread index within the half (0..255).
-template <int H, bool UPPER>
-__device__ __forceinline__ void inv_level(const float* S, float* X, int u, int bar) {
-  constexpr int CT = H / 16;            // 1, 2, 4
-  constexpr int TR = H / 4;             // row tiles per block
-  constexpr int PER = TR * (H / CT);    // threads per pair (64, 128, 256)
-  const int pair = u / PER, rem = u % PER;
-  const int r0 = 4 * (rem % TR), c0 = CT * (rem / TR);
-  const int o = pair * 2 * H;           // offset of the 2h block
-  float acc[4][CT] = {};
-  if (!UPPER) {
-    // T = L_BA Linv_AA -> X_BA slot
-    tile_mm<CT>(S + o * TLD + o + H, X + o * TLD + o, r0, c0, c0 & ~3, H, acc);
-    tile_store<CT>(X + o * TLD + o + H, r0, c0, acc);
-  } else {
-    // T = U_AB Uinv_BB -> X_AB slot
-    tile_mm<CT>(S + (o + H) * TLD + o, X + (o + H) * TLD + o + H, r0, c0, 0, (c0 + CT + 3) & ~3, acc);
-    tile_store<CT>(X + (o + H) * TLD + o, r0, c0, acc);
-  }
-  half_sync(bar);
-  float acc2[4][CT] = {};
-  if (!UPPER) {
-    // X_BA = -Linv_BB T
-    tile_mm<CT>(X + (o + H) * TLD + o + H, X + o * TLD + o + H, r0, c0, 0, r0 + 4, acc2);
-  } else {
-    // X_AB = -Uinv_AA T
-    tile_mm<CT>(X + o * TLD + o, X + (o + H) * TLD + o, r0, c0, r0, H, acc2);
-  }
-  half_sync(bar);
-  if (!UPPER) tile_store_neg<CT>(X + o * TLD + o + H, r0, c0, acc2);
-  else tile_store_neg<CT>(X + (o + H) * TLD + o, r0, c0, acc2);
-  half_sync(bar);
+// reciprocal: hardware approximation plus one Newton step (about 1 ulp)
+__device__ __forceinline__ float rcp_nr(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return fmaf(r, fmaf(-x, r, 1.f), r);
 }
 
-__global__ void __launch_bounds__(512) k_diag_tiled(float* __restrict__ A, int64_t ld, int k,
-                                                    float* __restrict__ Dinv, int* __restrict__ info) {
+__global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict__ A, int64_t ld, int k,
+                                                           float* __restrict__ Dinv, int* __restrict__ info) {
   extern __shared__ __align__(16) float dsm[];
-  float* S = dsm;                 // A -> L\U
-  float* Li = S + LU_NB * TLD;    // L^{-1}
-  float* Ui = Li + LU_NB * TLD;   // U^{-1}
+  float* S = dsm;                    // A -> L\U
+  float* Li = S + LU_NB * TLD;       // L^{-1}
+  float* Ui = Li + LU_NB * TLD;      // U^{-1}
+  float* rowbuf = Ui + LU_NB * TLD;  // [warp 0-3][2][16]
+  float* Ls = rowbuf + 4 * 32;       // 16 x 16 unit lower, column-major, ld 20
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
   float* Ab = A + off + off * ld;
+  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  float* Uo = Lo + LU_NB * LU_NB;
   {
     // 8 float4 per thread, all loads in flight before the first store
     float4 v[8];
@@ -724,89 +696,195 @@ __global__ void __launch_bounds__(512) k_diag_tiled(float* __restrict__ A, int64
   int bad = 0;
   for (int p = 0; p < LU_NB / DB; ++p) {
     const int jb = p * DB;
-    // F1
-    if (warp == 0) {
-      float P[4][DB];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int r = jb + lane + 32 * m;
-#pragma unroll
-        for (int c = 0; c < DB; ++c) P[m][c] = (r < LU_NB) ? S[(jb + c) * TLD + r] : 0.f;
-      }
+    // ---- A ----
+    if (warp < 4) {
+      float PT[DB], PB[DB];
+      const int rb = jb + DB + 32 * warp + lane;
+      const bool tv = lane < DB, bv = rb < LU_NB;
 #pragma unroll
       for (int c = 0; c < DB; ++c) {
-        const float piv = __shfl_sync(0xffffffffu, P[0][c], c);
+        PT[c] = tv ? S[(jb + c) * TLD + jb + lane] : 0.f;
+        PB[c] = bv ? S[(jb + c) * TLD + rb] : 0.f;
+      }
+      float* myrow = rowbuf + warp * 32;
+#pragma unroll
+      for (int c = 0; c < DB; ++c) {
+        float* rw = myrow + (c & 1) * DB;
+        if (lane == c) {
+#pragma unroll
+          for (int q4 = 0; q4 < DB; q4 += 4)
+            *(float4*)&rw[q4] = make_float4(PT[q4], PT[q4 + 1], PT[q4 + 2], PT[q4 + 3]);
+        }
+        __syncwarp();
+        float row[DB];
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4) {
+          const float4 v4 = *(const float4*)&rw[q4];
+          row[q4] = v4.x; row[q4 + 1] = v4.y; row[q4 + 2] = v4.z; row[q4 + 3] = v4.w;
+        }
+        const float piv = row[c];
         if (!(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
-        const float inv = 1.f / piv;
-        float uu[DB];
+        const float inv = rcp_nr(piv);
+        if (lane > c && tv) {
+          const float l = PT[c] * inv;
+          PT[c] = l;
 #pragma unroll
-        for (int c2 = c + 1; c2 < DB; ++c2) uu[c2] = __shfl_sync(0xffffffffu, P[0][c2], c);
+          for (int c2 = c + 1; c2 < DB; ++c2) PT[c2] = fmaf(-l, row[c2], PT[c2]);
+        }
+        if (bv) {
+          const float l = PB[c] * inv;
+          PB[c] = l;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          if (lane + 32 * m > c && jb + lane + 32 * m < LU_NB) {
-            const float l = P[m][c] * inv;
-            P[m][c] = l;
+          for (int c2 = c + 1; c2 < DB; ++c2) PB[c2] = fmaf(-l, row[c2], PB[c2]);
+        }
+      }
+      if (bv) {
 #pragma unroll
-            for (int c2 = c + 1; c2 < DB; ++c2) P[m][c2] -= l * uu[c2];
+        for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + rb] = PB[c];
+      }
+      if (warp == 0 && tv) {
+#pragma unroll
+        for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + jb + lane] = PT[c];
+      } else if (warp == 1) {
+        // inverse of the unit-lower 16 x 16 block, lane c < 16 solving for
+        // column c by column-oriented forward substitution
+        if (tv) {
+#pragma unroll
+          for (int q = 0; q < DB; ++q) Ls[q * 20 + lane] = PT[q];
+        }
+        __syncwarp();
+        float x[DB];
+#pragma unroll
+        for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int q = 0; q < DB - 1; ++q) {
+#pragma unroll
+          for (int i = q + 1; i < DB; ++i) x[i] = fmaf(-Ls[q * 20 + i], x[q], x[i]);
+        }
+        if (tv) {
+#pragma unroll
+          for (int i4 = 0; i4 < DB; i4 += 4)
+            *(float4*)&Li[(jb + lane) * TLD + jb + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
+        }
+      }
+    } else if (jb > 0) {
+      // T_L (16 x jb) into Li[p, <p] and T_U (jb x 16) into Ui[<p, p], on
+      // 4 x 1 tiles
+      const int nL = 4 * jb, nU = jb * 4;
+      for (int idx = t - 128; idx < nL + nU; idx += 384) {
+        float acc[4][1] = {};
+        if (idx < nL) {
+          const int r0 = 4 * (idx & 3), c = idx >> 2;
+          tile_mm<1>(S + jb, Li, r0, c, c & ~3, jb, acc);
+          tile_store<1>(Li + jb, r0, c, acc);
+        } else {
+          const int iu = idx - nL, c = iu & 15, r0 = 4 * (iu >> 4);
+          tile_mm<1>(Ui, S + jb * TLD, r0, c, r0, jb, acc);
+          tile_store<1>(Ui + jb * TLD, r0, c, acc);
+        }
+      }
+    }
+    __syncthreads();
+    // ---- B ----
+    if (t < 128) {
+      const int c = jb + DB + t;  // U block row, one thread per column
+      if (c < LU_NB) {
+        float v[DB], o[DB];
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4) {
+          const float4 a = *(const float4*)&S[c * TLD + jb + q4];
+          v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
+        }
+#pragma unroll
+        for (int i = 0; i < DB; ++i) o[i] = 0.f;
+#pragma unroll
+        for (int q = 0; q < DB; ++q) {
+#pragma unroll
+          for (int i4 = 0; i4 < DB; i4 += 4) {
+            const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
+            o[i4] = fmaf(l.x, v[q], o[i4]);
+            o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
+            o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
+            o[i4 + 3] = fmaf(l.w, v[q], o[i4 + 3]);
           }
         }
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4)
+          *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
       }
+    } else if (t < 256) {
+      const int c = t - 128;  // Linv[p, c] = -Linv_pp T_L[:, c]
+      if (c < jb) {
+        float v[DB], o[DB];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int r = jb + lane + 32 * m;
-        if (r < LU_NB) {
-#pragma unroll
-          for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + r] = P[m][c];
+        for (int q4 = 0; q4 < DB; q4 += 4) {
+          const float4 a = *(const float4*)&Li[c * TLD + jb + q4];
+          v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
         }
+#pragma unroll
+        for (int i = 0; i < DB; ++i) o[i] = 0.f;
+#pragma unroll
+        for (int q = 0; q < DB; ++q) {
+#pragma unroll
+          for (int i4 = 0; i4 < DB; i4 += 4) {
+            const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
+            o[i4] = fmaf(-l.x, v[q], o[i4]);
+            o[i4 + 1] = fmaf(-l.y, v[q], o[i4 + 1]);
+            o[i4 + 2] = fmaf(-l.z, v[q], o[i4 + 2]);
+            o[i4 + 3] = fmaf(-l.w, v[q], o[i4 + 3]);
+          }
+        }
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4)
+          *(float4*)&Li[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
       }
-      // inverse of the 16 x 16 unit-lower block: lane r owns row r
-      float X[DB];
+    } else if (warp == 12) {
+      // inverse of the upper 16 x 16 block, lane c < 16 solving for column
+      // c by column-oriented back substitution
+      float x[DB];
 #pragma unroll
-      for (int c = 0; c < DB; ++c) X[c] = (lane == c) ? 1.f : 0.f;
+      for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
 #pragma unroll
-      for (int q = 0; q < DB - 1; ++q) {
-        const float l = P[0][q];
+      for (int q = DB - 1; q >= 0; --q) {
+        const float* uc = S + (jb + q) * TLD + jb;
+        x[q] *= rcp_nr(uc[q]);
 #pragma unroll
-        for (int c = 0; c <= q; ++c) {
-          const float xq = __shfl_sync(0xffffffffu, X[c], q);
-          if (lane > q && lane < DB) X[c] -= l * xq;
-        }
+        for (int i = 0; i < q; ++i) x[i] = fmaf(-uc[i], x[q], x[i]);
       }
       if (lane < DB) {
 #pragma unroll
-        for (int c = 0; c < DB; ++c) Li[(jb + c) * TLD + jb + lane] = X[c];
+        for (int i4 = 0; i4 < DB; i4 += 4)
+          *(float4*)&Ui[(jb + lane) * TLD + jb + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
       }
     }
     __syncthreads();
-    if (jb + DB == LU_NB) break;
-    // F2: U block row, one thread per column
-    for (int c = jb + DB + t; c < LU_NB; c += 512) {
-      float v[DB], o[DB];
-#pragma unroll
-      for (int q4 = 0; q4 < DB; q4 += 4) {
-        const float4 a = *(const float4*)&S[c * TLD + jb + q4];
-        v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
-      }
-#pragma unroll
-      for (int i = 0; i < DB; ++i) o[i] = 0.f;
-#pragma unroll
-      for (int q = 0; q < DB; ++q) {
-#pragma unroll
-        for (int i4 = 0; i4 < DB; i4 += 4) {
-          const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
-          o[i4] = fmaf(l.x, v[q], o[i4]);
-          o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
-          o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
-          o[i4 + 3] = fmaf(l.w, v[q], o[i4 + 3]);
-        }
-      }
-#pragma unroll
-      for (int q4 = 0; q4 < DB; q4 += 4)
-        *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
-    }
-    __syncthreads();
-    // F3: trailing update on 4 x 4 tiles
+    // column block p of L\U and block row p of L^{-1} are final
     {
+      const int cs = jb + (t >> 5), r4 = 4 * (t & 31);
+      *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
+      const int cl = t >> 2, rl = jb + 4 * (t & 3);
+      *(float4*)(Lo + rl + cl * LU_NB) = *(const float4*)&Li[cl * TLD + rl];
+    }
+    // ---- C ----
+    if (t >= 256 && t < 384) {
+      const int r = t - 256;  // Uinv[r, p] = -T_U[r, :] Uinv_pp
+      if (r < jb) {
+        float v[DB], o[DB];
+#pragma unroll
+        for (int q = 0; q < DB; ++q) {
+          v[q] = Ui[(jb + q) * TLD + r];
+          o[q] = 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < DB; ++c) {
+#pragma unroll
+          for (int q = 0; q <= c; ++q) o[c] = fmaf(-v[q], Ui[(jb + c) * TLD + jb + q], o[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < DB; ++c) Ui[(jb + c) * TLD + r] = o[c];
+      }
+    }
+    if (jb + DB < LU_NB) {
       const int n = LU_NB - jb - DB, nt = n / 4;
       const float* Pb = S + jb * TLD + jb + DB;       // L21(r, q)
       const float* Qb = S + (jb + DB) * TLD + jb;     // U12(q, c)
@@ -824,65 +902,18 @@ __global__ void __launch_bounds__(512) k_diag_tiled(float* __restrict__ A, int64
       }
     }
     __syncthreads();
-  }
-  if (bad) atomicExch(info, k + 1);
-  if (warp < 8) {
-    // L^{-1}: its 16 x 16 diagonal inverses are in place
-    const int u = t;
-    inv_level<16, false>(S, Li, u, 1);
-    inv_level<32, false>(S, Li, u, 1);
-    inv_level<64, false>(S, Li, u, 1);
-  } else {
-    // U^{-1}: warp 8 + w inverts the 16 x 16 diagonal block w (lane = row)
+    // block column p of U^{-1} is final
     {
-      const int jb = (warp - 8) * DB;
-      float urow[DB], acc[DB];
-#pragma unroll
-      for (int c = 0; c < DB; ++c) {
-        urow[c] = (lane < DB) ? S[(jb + c) * TLD + jb + lane] : 0.f;
-        acc[c] = 0.f;
-      }
-#pragma unroll
-      for (int q = DB - 1; q >= 0; --q) {
-        const float uqq = __shfl_sync(0xffffffffu, urow[q], q);
-        const float inv = 1.f / uqq;
-#pragma unroll
-        for (int c = 0; c < DB; ++c) {
-          float x = (c >= q) ? (((c == q) ? 1.f : 0.f) + acc[c]) * inv : 0.f;
-          x = __shfl_sync(0xffffffffu, x, q);
-          if (lane == q) acc[c] = x;
-          else if (lane < q) acc[c] -= urow[q] * x;
-        }
-      }
-      if (lane < DB) {
-#pragma unroll
-        for (int c = 0; c < DB; ++c) Ui[(jb + c) * TLD + jb + lane] = acc[c];
-      }
+      const int cs = jb + (t >> 5), r4 = 4 * (t & 31);
+      *(float4*)(Uo + r4 + cs * LU_NB) = *(const float4*)&Ui[cs * TLD + r4];
     }
-    half_sync(2);
-    const int u = t - 256;
-    inv_level<16, true>(S, Ui, u, 2);
-    inv_level<32, true>(S, Ui, u, 2);
-    inv_level<64, true>(S, Ui, u, 2);
   }
-  __syncthreads();
-  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
-  float* Uo = Lo + LU_NB * LU_NB;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
-    *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&S[c * TLD + r4];
-    *(float4*)(Lo + r4 + c * LU_NB) = *(const float4*)&Li[c * TLD + r4];
-    *(float4*)(Uo + r4 + c * LU_NB) = *(const float4*)&Ui[c * TLD + r4];
+  if (warp == 0) {
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0 && bad) atomicExch(info, k + 1);
   }
 }
 
-// ---------------------------------------------------------------------------
-// Panels of one LU step in FP32 (CUDA cores): U12 = Linv A12 and
-// L21 = A21 Uinv, in place.  A CTA owns all 128 rows (U panel) or all 128
-// columns (L panel) of its 32-wide slice, so it reads its whole slice before
-// writing it back and slices never overlap.
-// ---------------------------------------------------------------------------
 constexpr int PW = 32;  // slice width
 constexpr int PANEL_SMEM = sizeof(float) * (LU_NB * TLD + LU_NB * (PW + 4));
 
@@ -978,8 +1009,7 @@ static void lu_attrs() {
   attr = true;
   cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float) * LU_NB * DLD));
-  cudaFuncSetAttribute(k_diag_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)(sizeof(float) * 3 * LU_NB * TLD));
+  cudaFuncSetAttribute(k_diag_factor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
   cudaFuncSetAttribute(k_gemm_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
   cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -992,7 +1022,7 @@ static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* in
                             cudaStream_t st) {
   const size_t kk = (size_t)k * LU_NB;
   const int rem = Npad - (int)kk - LU_NB;
-  k_diag_tiled<<<1, 512, sizeof(float) * 3 * LU_NB * TLD, st>>>(A, ld, k, Dinv, info);
+  k_diag_factor_tiled<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, Dinv, info);
   count_launches(1);
   if (rem <= 0) return;
   const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
@@ -1197,7 +1227,7 @@ namespace bem {
 // D1, D2 receive the two pairs of triangular inverses.
 void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, int* info, cudaStream_t st) {
   lu_attrs();
-  k_diag_tiled<<<1, 512, sizeof(float) * 3 * LU_NB * TLD, st>>>(A1, ld, 0, D1, info);
+  k_diag_factor_tiled<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, D1, info);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
   count_launches(2);
 }
