@@ -222,3 +222,70 @@ def solve_system(A, b, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 
     ctx.check(rc, "solve_system")
     return x, dict(iterations=st.iterations, rel_residual=st.rel_residual,
                    t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)
+
+
+def recover_strain_stress(dad: BEMdata, u=None, t=None, ctx: _lib.Context | None = None):
+    """Boundary strain and stress at the collocation nodes of a solved Kelvin
+    problem (`recover_strain_stress!`, src/Elasticity/StrainStress.jl:35-99):
+    (eps, sigma), n x 3 Voigt each; stored in dad.cache as strain, stress.
+    u, t default to the cached solution (`dad.u`, `dad.traction`)."""
+    pr = dad.properties
+    if not isinstance(pr, Elasticity):
+        raise ValueError("recover_strain_stress needs an elasticity problem")
+    if u is None or t is None:
+        if "u" not in dad.cache or "traction" not in dad.cache:
+            raise ValueError("no displacement/traction: call solve first")
+    u = np.ascontiguousarray(dad.cache["u"] if u is None else u, dtype=np.float64)
+    t = np.ascontiguousarray(dad.cache["traction"] if t is None else t, dtype=np.float64)
+    ctx = ctx or _lib.default_context()
+    g, keep = geom_struct(dad, device=False)
+    eps = np.zeros((dad.n, 3), order="F")
+    sig = np.zeros((dad.n, 3), order="F")
+    rc = ctx.L.bem_strain_stress2d(ctx.h, g, float(pr.lam), float(pr.mu), _ptr(u), _ptr(t),
+                                   _lib.BEM_MEM_HOST, _ptr(eps), _ptr(sig))
+    ctx.check(rc, "strain_stress")
+    dad.set_cache(strain=eps, stress=sig)
+    return eps, sig
+
+
+def hoop_stress(dad: BEMdata, center=(0.0, 0.0), sigma=None):
+    """sigma_theta_theta at the boundary nodes about `center` (polar rotation
+    of the recovered stress)."""
+    sig = dad.cache["stress"] if sigma is None else sigma
+    X = np.asarray(dad.collocation[: dad.n]) - np.asarray(center)
+    th = np.arctan2(X[:, 1], X[:, 0])
+    s, c = np.sin(th), np.cos(th)
+    return sig[:, 0] * s * s + sig[:, 1] * c * c - 2 * sig[:, 2] * s * c
+
+
+def kirsch_static(r, theta, a=1.0, sigma_inf=1.0):
+    """Static Kirsch stresses (sigma_rr, sigma_tt, sigma_rt) around a hole of
+    radius a under remote sigma_xx (data/elastico/iso/analytical_elastodynamics.jl:532-540)."""
+    r2 = (a / np.asarray(r)) ** 2
+    r4 = r2 * r2
+    srr = sigma_inf / 2 * (1 - r2) + sigma_inf / 2 * (1 - 4 * r2 + 3 * r4) * np.cos(2 * theta)
+    stt = sigma_inf / 2 * (1 + r2) - sigma_inf / 2 * (1 + 3 * r4) * np.cos(2 * theta)
+    srt = -sigma_inf / 2 * (1 + 2 * r2 - 3 * r4) * np.sin(2 * theta)
+    return srr, stt, srt
+
+
+def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib.Context | None = None):
+    """Laplace potential at interior points from the solved boundary data
+    (`interior_laplace`, src/Laplace/Lubrication.jl:399-416): every element
+    integrated with the near-field quadrature, T(p) = (g.q - h.T) / c."""
+    if not isinstance(dad.properties, Laplace):
+        raise ValueError("interior_laplace needs a Laplace problem")
+    if T is None or q is None:
+        if "T" not in dad.cache or "q" not in dad.cache:
+            raise ValueError("no boundary solution: call solve first")
+    pts = np.ascontiguousarray(np.asarray(pts, dtype=np.float64).reshape(-1, 2))
+    T = np.ascontiguousarray((dad.cache["T"] if T is None else T)[: dad.n], dtype=np.float64)
+    q = np.ascontiguousarray(dad.cache["q"] if q is None else q, dtype=np.float64)
+    xp, yp = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+    out = np.zeros(len(pts))
+    ctx = ctx or _lib.default_context()
+    g, keep = geom_struct(dad, device=False)
+    rc = ctx.L.bem_interior_laplace2d(ctx.h, g, float(dad.properties.k), int(npg), _ptr(T), _ptr(q),
+                                      len(pts), _ptr(xp), _ptr(yp), _lib.BEM_MEM_HOST, _ptr(out))
+    ctx.check(rc, "interior_laplace")
+    return out

@@ -385,6 +385,77 @@ def plate_with_hole(n_outer_el: int = 1024, n_hole_el: int = 342, p: int = 2, ha
 
 
 # ---------------------------------------------------------------------------
+# interior point grids (src/Core/InternalPoints.jl)
+# ---------------------------------------------------------------------------
+def _boundary_chords(dad: "BEMdata"):
+    """Element chords of the CAD nodes (or first/last field node)
+    (`_boundary_segments`, InternalPoints.jl:216-231)."""
+    if dad.ngeo >= 2:
+        g = np.asarray(dad.geo)
+        a, b = g[:, :-1].reshape(-1, 2), g[:, 1:].reshape(-1, 2)
+    else:
+        X = np.asarray(dad.collocation[: dad.n]).reshape(dad.ne, dad.p + 1, 2)
+        a, b = X[:, 0], X[:, -1]
+    return a, b
+
+
+def point_in_domain(dad: "BEMdata", pts) -> np.ndarray:
+    """Even-odd ray test against the boundary chords (`point_in_domain`,
+    `_inside_segments`, InternalPoints.jl:198-245)."""
+    P = np.atleast_2d(np.asarray(pts, np.float64))
+    a, b = _boundary_chords(dad)
+    px, py = P[:, 0:1], P[:, 1:2]
+    yi, yj = a[None, :, 1], b[None, :, 1]
+    cross = (yi > py) != (yj > py)
+    xint = (b[None, :, 0] - a[None, :, 0]) * (py - yi) / (yj - yi + 1e-30) + a[None, :, 0]
+    hits = np.sum(cross & (px < xint), axis=1)
+    return hits % 2 == 1
+
+
+def _dist_to_boundary(dad: "BEMdata", pts) -> np.ndarray:
+    """Distance to the piecewise-linear interpolant through each element's
+    CAD nodes (`_dist_to_boundary`, `_dist_element`, InternalPoints.jl:330-340,
+    Integration.jl:238-312)."""
+    P = np.atleast_2d(np.asarray(pts, np.float64))
+    a, b = _boundary_chords(dad)
+    ab = b - a
+    ap = P[:, None, :] - a[None, :, :]
+    t = np.clip(np.sum(ap * ab[None], -1) / (np.sum(ab * ab, -1)[None] + np.finfo(float).eps), 0, 1)
+    d = ap - t[..., None] * ab[None]
+    return np.sqrt(np.min(np.sum(d * d, -1), axis=1))
+
+
+def internal_grid(dad: "BEMdata", nx: int, ny: int, d_min: float = 0.01, layout: str = "gera") -> np.ndarray:
+    """Cartesian interior points in the boundary's bounding box, kept when
+    inside and at least d_min * (longest element) from the boundary
+    (`internal_grid`, InternalPoints.jl:23-42; layouts `_axis_nodes`, :62-73)."""
+    if nx < 1 or ny < 1:
+        raise ValueError("nx, ny must be >= 1")
+    X = np.asarray(dad.collocation[: dad.n])
+    if dad.ngeo:
+        X = np.concatenate([X, np.asarray(dad.geo).reshape(-1, 2)])
+    lo, hi = X.min(0), X.max(0)
+
+    def axis(n, lo_, hi_):
+        i = np.arange(1, n + 1)
+        if layout == "gera":
+            return lo_ + (hi_ - lo_) * i / (n + 1)
+        if layout == "cell":
+            return lo_ + (hi_ - lo_) * (i - 0.5) / n
+        if layout == "cheb":
+            return lo_ + (hi_ - lo_) * (1 - np.cos(np.pi * (i - 0.5) / n)) / 2
+        raise ValueError(f"layout must be gera, cell or cheb (got {layout})")
+
+    xs, ys = axis(nx, lo[0], hi[0]), axis(ny, lo[1], hi[1])
+    P = np.stack(np.meshgrid(xs, ys, indexing="xy"), -1).reshape(-1, 2)  # x fastest, as `for y, x`
+    keep = point_in_domain(dad, P)
+    clear = d_min * float(np.max(dad.elem_length))
+    if clear > 0:
+        keep &= _dist_to_boundary(dad, P) >= clear
+    return P[keep]
+
+
+# ---------------------------------------------------------------------------
 # analytic fields (src/Core/Analytical.jl)
 # ---------------------------------------------------------------------------
 @dataclass

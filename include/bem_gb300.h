@@ -213,6 +213,32 @@ int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, int npg, do
                                    void* cuda_stream);
 
 /*
+ * Laplace potential at m interior points from solved boundary data --
+ * replaces `interior_laplace(dad, pf; T, q)` (src/Laplace/Lubrication.jl:399-416;
+ * the same sum as `_interior_T`, test/laplace.jl:36-53): every element is
+ * integrated with the near-field quadrature of `integrate_element`
+ * (src/Core/Assembly_full.jl:262-289), T(p) = (g.q - h.T) / c, c = -sum h.
+ * T, q: the n boundary values (`dad.T[1:n]`, `dad.q`); xp, yp: point
+ * coordinates; out: m potentials.  mem says where T, q, xp, yp, out live.
+ */
+int bem_interior_laplace2d(bem_ctx* ctx, const bem_geom2d* geom, double k, int npg, const double* T,
+                           const double* q, int64_t m, const double* xp, const double* yp, int mem,
+                           double* out);
+
+/*
+ * Boundary strain and stress at the n collocation nodes of a solved Kelvin
+ * problem (Kane's method) -- replaces `recover_strain_stress!`
+ * (src/Elasticity/StrainStress.jl:35-53, 2-D branch `_recover_2d!`, :55-99).
+ * lam, mu: Lame constants of the effective 2-D model (`props.lambda`,
+ * `props.mu`, src/Core/Structures.jl:160-168).  u, t: node-major
+ * displacement and traction (2n each, `dad.u`, `dad.traction`).  eps, sigma:
+ * n x 3 column-major Voigt (e11, e22, g12) and (s11, s22, s12), as the
+ * reference's `zeros(n, 3)`.  mem says where u, t, eps and sigma live.
+ */
+int bem_strain_stress2d(bem_ctx* ctx, const bem_geom2d* geom, double lam, double mu, const double* u,
+                        const double* t, int mem, double* eps, double* sigma);
+
+/*
  * Built-in consistency check of the tensor-core paths (no reference
  * counterpart).  which = 1: factor an n x n test matrix (n a multiple of 128)
  * once with the tcgen05 trailing updates and once with the legacy mma.sync

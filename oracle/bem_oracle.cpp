@@ -1384,6 +1384,78 @@ int orc_near_element(const double* xy, int nn, double L, double pfx, double pfy,
 // 152-174): A = H with BC==0 columns replaced by -G[:,j];
 // b = sum_{BC==0} -H[:,j] BV_j + sum_{BC!=0} G[:,j] BV_j.
 // rows x rows A, cols = number of boundary DOFs.
+// interior_laplace (src/Laplace/Lubrication.jl:399-416): potential at m
+// interior points, every element through integrate_element.
+int orc_interior_laplace(const OrcGeom* og, double k, int npg, int nearfield, const double* T,
+                         const double* q, int m, const double* xp, const double* yp, double* out) {
+  Geom gg = to_geom(og);
+  Ctx C;
+  setup_ctx(C, &gg, npg);
+  C.prob.kind = 0;
+  C.prob.k = k;
+  C.nearfield = nearfield;
+  C.singular = 0;
+  const int nn = gg.p + 1;
+#pragma omp parallel for schedule(static)
+  for (int p = 0; p < m; ++p) {
+    std::vector<double> h(nn), g(nn);
+    double gt = 0.0, hs = 0.0;
+    for (int e = 0; e < gg.ne; ++e) {
+      integrate_element(C, e, V2{xp[p], yp[p]}, -1, h.data(), g.data());
+      for (int a = 0; a < nn; ++a) {
+        const int j = e * nn + a;
+        gt += g[a] * q[j] - h[a] * T[j];
+        hs += h[a];
+      }
+    }
+    out[p] = gt / (-hs);
+  }
+  return 0;
+}
+
+// recover_strain_stress! 2-D (src/Elasticity/StrainStress.jl:55-99): Kane's
+// boundary strain/stress per collocation node; eps, sig n x 3 column-major.
+void orc_strain_stress2d(const OrcGeom* og, double lam, double mu, const double* u, const double* t,
+                         double* eps, double* sig) {
+  const Geom g = to_geom(og);
+  const Poly P = make_legendre(g.p);
+  const int nn = g.p + 1, n = g.n;
+  std::vector<double> N(nn), dN(nn);
+  for (int i = 0; i < 3 * n; ++i) eps[i] = sig[i] = 0.0;
+  for (int e = 0; e < g.ne; ++e) {
+    for (int k = 0; k < nn; ++k) {
+      shapefun(P, P.nodes[k], N.data(), dN.data());
+      double dx0 = 0, dx1 = 0, du0 = 0, du1 = 0;
+      for (int j = 0; j < nn; ++j) {
+        const int ja = e * nn + j;
+        dx0 += dN[j] * g.px[ja];
+        dx1 += dN[j] * g.py[ja];
+        du0 += dN[j] * u[2 * ja];
+        du1 += dN[j] * u[2 * ja + 1];
+      }
+      const int i = e * nn + k;
+      const double nlen = std::hypot(g.nx[i], g.ny[i]);
+      const double n1 = g.nx[i] / nlen, n2 = g.ny[i] / nlen, t1 = -n2, t2 = n1;
+      const double Jproj = t1 * dx0 + t2 * dx1;
+      if (std::fabs(Jproj) < 1e-16) continue;
+      const double dudt0 = du0 / Jproj, dudt1 = du1 / Jproj;
+      const double ess = t1 * dudt0 + t2 * dudt1;
+      const double tv0 = t[2 * i], tv1 = t[2 * i + 1];
+      const double snn = n1 * tv0 + n2 * tv1, snt = t1 * tv0 + t2 * tv1;
+      const double den = lam + 2 * mu;
+      if (std::fabs(den) < 1e-30) continue;
+      const double enn = (snn - lam * ess) / den, ent = snt / (2 * mu);
+      const double sss = lam * (enn + ess) + 2 * mu * ess;
+      eps[i] = enn * n1 * n1 + ess * t1 * t1 + 2 * ent * n1 * t1;
+      eps[i + n] = enn * n2 * n2 + ess * t2 * t2 + 2 * ent * n2 * t2;
+      eps[i + 2 * n] = 2 * (enn * n1 * n2 + ess * t1 * t2 + ent * (n1 * t2 + n2 * t1));
+      sig[i] = snn * n1 * n1 + sss * t1 * t1 + 2 * snt * n1 * t1;
+      sig[i + n] = snn * n2 * n2 + sss * t2 * t2 + 2 * snt * n2 * t2;
+      sig[i + 2 * n] = snn * n1 * n2 + sss * t1 * t2 + snt * (n1 * t2 + n2 * t1);
+    }
+  }
+}
+
 void orc_apply_bc(int64_t rows, int64_t cols, const double* H, const double* G, const int32_t* BC,
                   const double* BV, double* A, double* b) {
   std::memcpy(A, H, sizeof(double) * rows * rows);

@@ -39,8 +39,7 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
+        build()  # make: rebuilds only when the source is newer than the library
         _lib = ctypes.CDLL(LIB_PATH)
         d = ctypes.c_double
         P = ctypes.POINTER(d)
@@ -74,6 +73,9 @@ def lib():
         _lib.orc_near_element.restype = i
         _lib.orc_apply_bc.argtypes = [ctypes.c_int64, ctypes.c_int64, P, P,
                                       ctypes.POINTER(ctypes.c_int32), P, P, P]
+        _lib.orc_strain_stress2d.argtypes = [ctypes.POINTER(OrcGeom), d, d, P, P, P, P]
+        _lib.orc_interior_laplace.argtypes = [ctypes.POINTER(OrcGeom), d, i, i, P, P, i, P, P, P]
+        _lib.orc_interior_laplace.restype = i
     return _lib
 
 
@@ -183,6 +185,32 @@ def split_sol(dad, x):
     t = np.where(BC == 0, x[:nb], BV)
     dad.set_cache(u=u, traction=t, T=u, x=np.asarray(x))
     return u
+
+
+def interior_laplace(dad, pts, npg=16, nearfield="tanp3c", T=None, q=None):
+    """Potential at interior points (`interior_laplace`, src/Laplace/Lubrication.jl:399-416)."""
+    pts = np.ascontiguousarray(np.asarray(pts, dtype=np.float64).reshape(-1, 2))
+    T = np.ascontiguousarray((dad.cache["T"] if T is None else T)[: dad.n], dtype=np.float64)
+    q = np.ascontiguousarray(dad.cache["q"] if q is None else q, dtype=np.float64)
+    xp, yp = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+    out = np.zeros(len(pts))
+    g, keep = make_geom(dad)
+    lib().orc_interior_laplace(ctypes.byref(g), float(dad.properties.k), int(npg), NEARFIELD[nearfield],
+                               _p(T), _p(q), len(pts), _p(xp), _p(yp), _p(out))
+    return out
+
+
+def strain_stress(dad, u=None, t=None):
+    """Kane boundary strain/stress, n x 3 each (`recover_strain_stress!`,
+    src/Elasticity/StrainStress.jl:35-99)."""
+    u = np.ascontiguousarray(dad.cache["u"] if u is None else u, dtype=np.float64)
+    t = np.ascontiguousarray(dad.cache["traction"] if t is None else t, dtype=np.float64)
+    g, keep = make_geom(dad)
+    eps = np.zeros((dad.n, 3), order="F")
+    sig = np.zeros((dad.n, 3), order="F")
+    pr = dad.properties
+    lib().orc_strain_stress2d(ctypes.byref(g), float(pr.lam), float(pr.mu), _p(u), _p(t), _p(eps), _p(sig))
+    return eps, sig
 
 
 def solve(dad):

@@ -1,0 +1,61 @@
+"""Interior potential on the GPU (bem_interior_laplace2d) against the oracle,
+the reference's near-field approach test, and a curved domain against the
+analytic field."""
+import numpy as np
+import pytest
+
+from bem_gmsh_gb300 import quadrado, star_domain, internal_grid
+from bem_gmsh_gb300.geometry import ana_laplace_linear, ana_laplace_expcos, attach_analytical
+from bem_gmsh_gb300.api import solve, interior_laplace
+
+pytestmark = pytest.mark.gpu
+
+
+def test_interior_matches_oracle(orc):
+    dad = star_domain(200, p=2, seed=9)
+    orc.assemble(dad, npg=16)
+    orc.solve(dad)
+    T, q = dad.cache["T"], dad.cache["q"]
+    pts = internal_grid(dad, 12, 12)
+    pts = np.concatenate([pts, [[0.0, 0.0]]])
+    ref = orc.interior_laplace(dad, pts, npg=16, T=T, q=q)
+    got = interior_laplace(dad, pts, npg=16, T=T, q=q)
+    # per point: max(1e-11, 10x the oracle's own change when every coordinate
+    # (point and geometry) moves by one ulp).  Points close to the boundary
+    # meet the conditioning of the near-field map; there the GPU's fused
+    # multiply-adds (the reference and the oracle round every product) move
+    # single values by up to ~1.5e-12 relative.  1e-11 stays inside the
+    # 1e-10 FP64 bar of the pipeline.
+    from test_gpu_assembly import perturbed
+    sens = np.zeros(len(pts))
+    for seed in range(3):
+        ref_p = orc.interior_laplace(perturbed(dad, seed), np.nextafter(pts, np.inf if seed % 2 else -np.inf),
+                                     npg=16, T=T, q=q)
+        sens = np.maximum(sens, np.abs(ref_p - ref))
+    scale = np.max(np.abs(ref))
+    tol = np.maximum(1e-11 * scale, 10 * sens)
+    assert np.all(np.abs(got - ref) <= tol), np.max(np.abs(got - ref) / tol)
+    # almost every point agrees to rounding
+    assert np.mean(np.abs(got - ref) <= 1e-13 * scale) > 0.9
+
+
+def test_interior_approach_gpu():
+    """test/laplace.jl:55-86 (tanp3c): |T(0.5, d) - 0.5| < 5e-3, d -> 1e-6."""
+    dad = quadrado(ndiv=20, pontointerno=False)
+    attach_analytical(dad, ana_laplace_linear((1.0, 0.0)))
+    solve(dad, npg=16, mode="fp64")
+    ds = [1e-1, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6]
+    T = interior_laplace(dad, [[0.5, d] for d in ds], npg=16)
+    assert np.max(np.abs(T - 0.5)) < 5e-3, T
+
+
+def test_interior_star_analytic():
+    """Curved quadratic boundary, T = e^x cos y: interior values from the
+    mixed-precision solve follow the analytic field."""
+    dad = star_domain(900, p=2, seed=2)
+    ana = ana_laplace_expcos()
+    solve(dad, npg=16, mode="mixed")
+    pts = internal_grid(dad, 20, 20, d_min=0.5)
+    T = interior_laplace(dad, pts, npg=16)
+    exact = np.exp(pts[:, 0]) * np.cos(pts[:, 1])
+    assert np.max(np.abs(T - exact)) < 5e-4 * np.max(np.abs(exact))
