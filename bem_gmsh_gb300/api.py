@@ -12,6 +12,8 @@ ABI of libbem_gb300.so; there is no CPU path.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -289,3 +291,55 @@ def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib
                                       len(pts), _ptr(xp), _ptr(yp), _lib.BEM_MEM_HOST, _ptr(out))
     ctx.check(rc, "interior_laplace")
     return out
+
+
+def solve_batch(dads, npg: int = 20, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 200,
+                near_factor: float = 1.5, nworkers: int = 8, ctx: _lib.Context | None = None,
+                return_stats: bool = False):
+    """`solve(dad)` for many independent domains in one call
+    (bem_solve2d_batch): every domain is assembled and solved on the GPU;
+    worker threads with their own streams overlap the domains.  All domains
+    share the physics of the first one.  Returns the list of solution
+    vectors (and the per-domain stats)."""
+    dads = list(dads)
+    if not dads:
+        return ([], []) if return_stats else []
+    ctx = ctx or _lib.default_context()
+    pr = dads[0].properties
+    kind = 0 if isinstance(pr, Laplace) else 1
+    for d in dads:
+        if type(d.properties) is not type(pr) or d.properties != pr:
+            raise ValueError("solve_batch: all domains need the same physics")
+    dof = pr.ndof
+    geoms = (_lib.BemGeom2D * len(dads))()
+    keep = []
+    for i, d in enumerate(dads):
+        g, k = geom_struct(d, device=False)
+        geoms[i] = g
+        keep.append(k)
+    bc_len = [dof * d.n for d in dads]
+    x_len = [dof * d.nt for d in dads]
+    bc_off = np.concatenate([[0], np.cumsum(bc_len)[:-1]]).astype(np.int64)
+    x_off = np.concatenate([[0], np.cumsum(x_len)[:-1]]).astype(np.int64)
+    BC = np.ascontiguousarray(np.concatenate([np.asarray(d.BC, np.int32) for d in dads]))
+    BV = np.ascontiguousarray(np.concatenate([np.asarray(d.BV, np.float64) for d in dads]))
+    x = np.zeros(int(sum(x_len)))
+    stats = (_lib.BemSolveStats * len(dads))()
+    p0 = float(pr.k) if kind == 0 else float(pr.mu)
+    p1 = 0.0 if kind == 0 else float(pr.nu_eff)
+    rc = ctx.L.bem_solve2d_batch(ctx.h, len(dads), geoms, kind, p0, p1, _ptr(BC), _ptr(BV),
+                                 bc_off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(npg),
+                                 float(near_factor), _MODES[mode], float(tol), int(max_iter),
+                                 _lib.BEM_MEM_HOST, _ptr(x),
+                                 x_off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(nworkers), stats)
+    if rc not in (_lib.BEM_OK, 4):
+        ctx.check(rc, "solve_batch")
+    xs = [x[o:o + n].copy() for o, n in zip(x_off, x_len)]
+    for d, xi in zip(dads, xs):
+        split_sol(d, xi)
+    if return_stats:
+        st = [dict(status=s.status, iterations=s.iterations, rel_residual=s.rel_residual,
+                   t_assemble_ms=s.t_assemble_ms, t_factor_ms=s.t_factor_ms, t_refine_ms=s.t_refine_ms)
+              for s in stats]
+        return xs, st
+    return xs

@@ -181,8 +181,11 @@ extern "C" int bem_ctx_create(int device, bem_ctx** out) {
 
 extern "C" int bem_ctx_destroy(bem_ctx* c) {
   if (!c) return BEM_ERR_INVALID;
+  for (bem_ctx* w : c->workers) bem_ctx_destroy(w);
+  c->workers.clear();
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  bem_release_solver(c);
   for (auto& b : c->slots)
     if (b.p) cudaFree(b.p);
   c->prof.release();

@@ -32,6 +32,8 @@ struct bem_ctx {
   int pair_cap_hint = 0;
   int opt_tcgen05 = 1;  // BEM_OPT_TCGEN05: trailing updates on tcgen05
   int opt_far_df = 1;   // BEM_OPT_FAR_DF
+  void* cusolver_handle = nullptr;  // FP64 comparison path (created on first use)
+  std::vector<bem_ctx*> workers;    // sub-contexts of batched calls (own streams)
   bem::KProf prof;      // BEM_OPT_KERNEL_TIMING
 
   // second stream and events of the lookahead LU (created on first use)
@@ -62,6 +64,7 @@ struct CallScope {
 };
 
 int bem_check_geom(const bem_geom2d* g, int npg, double near_factor);
+void bem_release_solver(bem_ctx* c);
 // host-side rule tables of an assembly (element Gauss weights on the host)
 void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, bem::Rules& R);
 int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, bem::GeomDev& gd,

@@ -12,6 +12,7 @@
 // precondition an FP64 GMRES whose residual uses the FP64 matrix, so the
 // final solution has FP64 accuracy.
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "bem_lu.h"
@@ -1003,10 +1004,12 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Linv, 
   }
 }
 
+static void lu_attrs_once();
 static void lu_attrs() {
-  static bool attr = false;
-  if (attr) return;
-  attr = true;
+  static std::once_flag once;
+  std::call_once(once, lu_attrs_once);
+}
+static void lu_attrs_once() {
   cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float) * LU_NB * DLD));
   cudaFuncSetAttribute(k_diag_factor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
@@ -1132,8 +1135,9 @@ static void lu_solve_vec_steps(const float* A, int64_t ld, int Npad, const float
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
                  float* out, int* flags, int* err, cudaStream_t st) {
   const int K = Npad / LU_NB;
-  static int max_coresident = -1;
-  if (max_coresident < 0) {
+  static int max_coresident = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
     int dev = 0, nsm = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1142,7 +1146,7 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
     cudaFuncSetAttribute(k_trsv_wave<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_trsv_wave<false>, 256, dsm);
     max_coresident = nsm * per;
-  }
+  });
   const size_t dsm = sizeof(float) * LU_NB * (LU_NB + 1);
   if (K > max_coresident) {  // too many block rows to keep resident: step-wise launches
     lu_solve_vec_steps(A, ld, Npad, Dinv, r, tmp, st);

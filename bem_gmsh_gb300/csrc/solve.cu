@@ -5,6 +5,7 @@
 // Replaces `solve(dad)` = `applyBC` + `bem_linsolve` (src/Core/Solver.jl:24-64,
 // 114-131; src/Core/LinearSolveUtils.jl:44-49) for dense systems.
 #include <dlfcn.h>
+#include <mutex>
 
 #include <cmath>
 #include <cstring>
@@ -28,36 +29,37 @@ struct Cusolver {
   using Getrf = int (*)(void*, int, int, double*, int, double*, int*, int*);
   using Getrs = int (*)(void*, int, int, int, const double*, int, const int*, double*, int, int*);
   void* so = nullptr;
-  void* handle = nullptr;
+  bool loaded = false;
   Create create = nullptr;
   Destroy destroy = nullptr;
   SetStream set_stream = nullptr;
   BufSize bufsize = nullptr;
   Getrf getrf = nullptr;
   Getrs getrs = nullptr;
-  bool ok() const { return handle != nullptr; }
+  bool ok() const { return loaded; }
 };
 
+// cuSOLVER entry points, resolved once per process (thread-safe); each
+// context creates its own handle (handles are not shared across threads)
 Cusolver* cusolver() {
   static Cusolver cs;
-  static bool tried = false;
-  if (tried) return cs.ok() ? &cs : nullptr;
-  tried = true;
-  const char* names[] = {"libcusolver.so.12", "libcusolver.so.13", "libcusolver.so",
-                         "/usr/local/cuda/lib64/libcusolver.so.12", "/usr/local/cuda/lib64/libcusolver.so"};
-  for (const char* n : names) {
-    cs.so = dlopen(n, RTLD_NOW | RTLD_LOCAL);
-    if (cs.so) break;
-  }
-  if (!cs.so) return nullptr;
-  cs.create = (Cusolver::Create)dlsym(cs.so, "cusolverDnCreate");
-  cs.destroy = (Cusolver::Destroy)dlsym(cs.so, "cusolverDnDestroy");
-  cs.set_stream = (Cusolver::SetStream)dlsym(cs.so, "cusolverDnSetStream");
-  cs.bufsize = (Cusolver::BufSize)dlsym(cs.so, "cusolverDnDgetrf_bufferSize");
-  cs.getrf = (Cusolver::Getrf)dlsym(cs.so, "cusolverDnDgetrf");
-  cs.getrs = (Cusolver::Getrs)dlsym(cs.so, "cusolverDnDgetrs");
-  if (!cs.create || !cs.set_stream || !cs.bufsize || !cs.getrf || !cs.getrs) return nullptr;
-  if (cs.create(&cs.handle) != 0) cs.handle = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const char* names[] = {"libcusolver.so.12", "libcusolver.so.13", "libcusolver.so",
+                           "/usr/local/cuda/lib64/libcusolver.so.12", "/usr/local/cuda/lib64/libcusolver.so"};
+    for (const char* n : names) {
+      cs.so = dlopen(n, RTLD_NOW | RTLD_LOCAL);
+      if (cs.so) break;
+    }
+    if (!cs.so) return;
+    cs.create = (Cusolver::Create)dlsym(cs.so, "cusolverDnCreate");
+    cs.destroy = (Cusolver::Destroy)dlsym(cs.so, "cusolverDnDestroy");
+    cs.set_stream = (Cusolver::SetStream)dlsym(cs.so, "cusolverDnSetStream");
+    cs.bufsize = (Cusolver::BufSize)dlsym(cs.so, "cusolverDnDgetrf_bufferSize");
+    cs.getrf = (Cusolver::Getrf)dlsym(cs.so, "cusolverDnDgetrf");
+    cs.getrs = (Cusolver::Getrs)dlsym(cs.so, "cusolverDnDgetrs");
+    cs.loaded = cs.create && cs.destroy && cs.set_stream && cs.bufsize && cs.getrf && cs.getrs;
+  });
   return cs.ok() ? &cs : nullptr;
 }
 
@@ -90,6 +92,12 @@ double dev_dot(bem_ctx* c, const double* v, const double* w, int N, double* hbuf
 }
 
 }  // namespace
+
+void bem_release_solver(bem_ctx* c) {
+  Cusolver* cs = cusolver();
+  if (cs && c->cusolver_handle) cs->destroy(c->cusolver_handle);
+  c->cusolver_handle = nullptr;
+}
 
 // ---------------------------------------------------------------------------
 // mixed precision: FP32 LU (3xTF32 updates) preconditioning FP64 FGMRES
@@ -257,25 +265,29 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
 int bem_solve_fp64_dev(bem_ctx* c, int N, double* A64, int64_t lda, const double* b, double* x,
                        bem_solve_stats* stats) {
   Cusolver* cs = cusolver();
-  if (!cs) {
+  if (cs && !c->cusolver_handle) {
+    void* h = nullptr;
+    if (cs->create(&h) == 0) c->cusolver_handle = h;
+  }
+  if (!cs || !c->cusolver_handle) {
     c->last_error = "cuSOLVER could not be loaded for the FP64 comparison path";
     return BEM_ERR_UNSUPPORTED;
   }
   cudaStream_t st = c->stream;
-  cs->set_stream(cs->handle, st);
+  cs->set_stream(c->cusolver_handle, st);
   int lwork = 0;
-  if (cs->bufsize(cs->handle, N, N, A64, (int)lda, &lwork) != 0) return BEM_ERR_CUDA;
+  if (cs->bufsize(c->cusolver_handle, N, N, A64, (int)lda, &lwork) != 0) return BEM_ERR_CUDA;
   double* work = (double*)c->get(bem_ctx::SLOT_LU3, sizeof(double) * ((size_t)lwork + 16));
   int* ipiv = (int*)c->get(bem_ctx::SLOT_LU4, sizeof(int) * ((size_t)N + 16));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
   if (!work || !ipiv || !info) return BEM_ERR_NOMEM;
   Timer tf, tr;
   tf.start(st);
-  if (cs->getrf(cs->handle, N, N, A64, (int)lda, work, ipiv, info) != 0) return BEM_ERR_CUDA;
+  if (cs->getrf(c->cusolver_handle, N, N, A64, (int)lda, work, ipiv, info) != 0) return BEM_ERR_CUDA;
   tf.stop(st);
   tr.start(st);
   cudaMemcpyAsync(x, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, st);
-  if (cs->getrs(cs->handle, 0, N, 1, A64, (int)lda, ipiv, x, N, info + 1) != 0) return BEM_ERR_CUDA;
+  if (cs->getrs(c->cusolver_handle, 0, N, 1, A64, (int)lda, ipiv, x, N, info + 1) != 0) return BEM_ERR_CUDA;
   tr.stop(st);
   int hi[2] = {0, 0};
   cudaMemcpyAsync(hi, info, sizeof(hi), cudaMemcpyDeviceToHost, st);

@@ -213,6 +213,23 @@ int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, int npg, do
                                    void* cuda_stream);
 
 /*
+ * Batched solves of ndom independent domains with uneven sizes (the
+ * reference solves one mesh per `solve(dad)` call, src/Core/Solver.jl:24-64;
+ * there is no batched counterpart).  Domain d is geoms[d]; its BC/BV entries
+ * start at BC + bc_off[d], BV + bc_off[d] (dof * n_d of them) and its solution
+ * is written to x + x_off[d] (dof * nt_d values).  Every domain runs the
+ * bem_solve2d pipeline (same arguments for all); nworkers host threads, each
+ * with its own stream and workspace, take domains largest first (0 = 8,
+ * at most 32).  stats (optional) receives one record per domain.  Returns
+ * the first error met, BEM_ERR_NOT_CONVERGED if a domain stopped short of
+ * tol, else BEM_OK.  The call is synchronous.
+ */
+int bem_solve2d_batch(bem_ctx* ctx, int ndom, const bem_geom2d* geoms, int kind, double prm0, double prm1,
+                      const int32_t* BC, const double* BV, const int64_t* bc_off, int npg, double near_factor,
+                      int mode, double tol, int max_iter, int mem, double* x, const int64_t* x_off,
+                      int nworkers, bem_solve_stats* stats);
+
+/*
  * Laplace potential at m interior points from solved boundary data --
  * replaces `interior_laplace(dad, pf; T, q)` (src/Laplace/Lubrication.jl:399-416;
  * the same sum as `_interior_T`, test/laplace.jl:36-53): every element is
