@@ -343,3 +343,35 @@ def solve_batch(dads, npg: int = 20, mode: str = "mixed", tol: float = 1e-14, ma
               for s in stats]
         return xs, st
     return xs
+
+
+def adjoint_laplace(dad: BEMdata, q_target, npg: int = 16, near_factor: float = 1.5, tol: float = 1e-14,
+                    max_iter: int = 200, ctx: _lib.Context | None = None, return_stats: bool = False):
+    """J = 1/2 sum_{BC=0} (q - q_target)^2 and its gradient dJ/d(node x, y),
+    (n, 2), by the adjoint method through assembly and the mixed-precision
+    solve (bem_adjoint_laplace2d).  `dad` must take its element geometry from
+    its nodes (`from_nodes`)."""
+    if not isinstance(dad.properties, Laplace):
+        raise ValueError("adjoint_laplace needs a Laplace problem")
+    if dad.ngeo != 0 or dad.nt != dad.n:
+        raise ValueError("adjoint_laplace needs node-interpolant elements (from_nodes) and no internal points")
+    ctx = ctx or _lib.default_context()
+    g, keep = geom_struct(dad, device=False)
+    BC = np.ascontiguousarray(dad.BC, dtype=np.int32)
+    BV = np.ascontiguousarray(dad.BV, dtype=np.float64)
+    qt = np.ascontiguousarray(q_target, dtype=np.float64)
+    if qt.shape != (dad.n,):
+        raise ValueError("q_target must have one value per boundary node")
+    J = ctypes.c_double()
+    grad = np.zeros(2 * dad.n)
+    st = _lib.BemSolveStats()
+    rc = ctx.L.bem_adjoint_laplace2d(ctx.h, g, float(dad.properties.k), _ptr(BC), _ptr(BV), _ptr(qt), int(npg),
+                                     float(near_factor), float(tol), int(max_iter), _lib.BEM_MEM_HOST,
+                                     ctypes.byref(J), _ptr(grad), ctypes.byref(st))
+    if rc not in (_lib.BEM_OK, 4):
+        ctx.check(rc, "adjoint_laplace")
+    out = (J.value, grad.reshape(dad.n, 2))
+    if return_stats:
+        return out + (dict(status=st.status, iterations=st.iterations, t_assemble_ms=st.t_assemble_ms,
+                           t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms),)
+    return out

@@ -1004,6 +1004,81 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Linv, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Thin look-ahead updates of one LU step in FP32 on the CUDA cores, both in
+// one launch: block column k+1 (C: rem x 128) and block row k+1 (C: 128 x
+// rem-128) get C -= L21 U12 with K = 128.  64 x 64 tiles, operands staged by
+// cp.async, 4 x 4 register tiles; a 1-D grid lists the tiles of both parts.
+// ---------------------------------------------------------------------------
+constexpr int TT = 64;
+constexpr int TPLD = TT + 4;      // staged L: [q][r]
+constexpr int TQLD = LU_NB + 4;   // staged U: [c][q]
+constexpr int THIN_SMEM = (int)sizeof(float) * (LU_NB * TPLD + TT * TQLD);
+
+__global__ void __launch_bounds__(256) k_thin_update(float* A, int64_t ld, int kk, int rem) {
+  extern __shared__ __align__(16) float tsm[];
+  float* Ps = tsm;                  // Ps[q * TPLD + r] = L21(m0 + r, q)
+  float* Qs = tsm + LU_NB * TPLD;   // Qs[c * TQLD + q] = U12(q, n0 + c)
+  const int t = threadIdx.x;
+  const int ncol = (rem / TT) * (LU_NB / TT);
+  int tile = blockIdx.x, z = 0;
+  if (tile >= ncol) { tile -= ncol; z = 1; }
+  const int M = z == 0 ? rem : LU_NB;
+  const int mt = M / TT;
+  const int m0 = (tile % mt) * TT, n0 = (tile / mt) * TT;
+  const int co = z == 0 ? 0 : LU_NB;
+  const size_t r_abs = (size_t)kk + LU_NB + m0, c_abs = (size_t)kk + LU_NB + co + n0;
+  float* C = A + r_abs + c_abs * ld;
+  const float* L = A + r_abs + (size_t)kk * ld;
+  const float* U = A + (size_t)kk + c_abs * ld;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int idx = t + 256 * i;
+    const int q = idx >> 4, r4 = 4 * (idx & 15);
+    cp_async16(&Ps[q * TPLD + r4], L + r4 + (size_t)q * ld);
+    const int c = idx >> 5, q4 = 4 * (idx & 31);
+    cp_async16(&Qs[c * TQLD + q4], U + q4 + (size_t)c * ld);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int r0 = 4 * (t & 15), c0 = 4 * (t >> 4);
+  float acc[4][4] = {};
+#pragma unroll 4
+  for (int q = 0; q < LU_NB; q += 4) {
+    float4 pv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) pv[i] = *(const float4*)&Ps[(q + i) * TPLD + r0];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float4 qv = *(const float4*)&Qs[(c0 + j) * TQLD + q];
+      const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        acc[0][j] = fmaf(pv[i].x, qq[i], acc[0][j]);
+        acc[1][j] = fmaf(pv[i].y, qq[i], acc[1][j]);
+        acc[2][j] = fmaf(pv[i].z, qq[i], acc[2][j]);
+        acc[3][j] = fmaf(pv[i].w, qq[i], acc[3][j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    float4* cp = (float4*)(C + r0 + (size_t)(c0 + j) * ld);
+    float4 cv = *cp;
+    cv.x -= acc[0][j];
+    cv.y -= acc[1][j];
+    cv.z -= acc[2][j];
+    cv.w -= acc[3][j];
+    *cp = cv;
+  }
+}
+
+static void thin_update(float* A, int64_t ld, int k, int rem, cudaStream_t st) {
+  const int tiles = (rem / TT) * (LU_NB / TT) + (LU_NB / TT) * ((rem - LU_NB) / TT);
+  k_thin_update<<<tiles, 256, THIN_SMEM, st>>>(A, ld, k * LU_NB, rem);
+  count_launches(1);
+}
+
 static void lu_attrs_once();
 static void lu_attrs() {
   static std::once_flag once;
@@ -1018,6 +1093,7 @@ static void lu_attrs_once() {
   cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
   cudaFuncSetAttribute(k_panels, cudaFuncAttributeMaxDynamicSharedMemorySize, PANEL_SMEM);
+  cudaFuncSetAttribute(k_thin_update, cudaFuncAttributeMaxDynamicSharedMemorySize, THIN_SMEM);
 }
 
 // diagonal block k and its two panels: U12 = Linv A12, L21 = A21 Uinv
@@ -1062,10 +1138,11 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
 }
 
 // Lookahead-1 schedule on two streams.  `la` (the critical path) finishes
-// the thin part of step k's update -- block column k+1 and block row k+1 --
-// then factors diagonal block k+1, its panels and split parts; `st` runs the
-// bulk of step k's trailing update meanwhile.  evP[k]: panels/splits of step
-// k ready; evT[k]: bulk update of step k done.  tc[2]: plans with separate
+// the thin part of step k's update -- block column k+1 and block row k+1,
+// one FP32 launch -- then factors diagonal block k+1 and its panels; `st`
+// splits step k's panels into the tensor-core operands and runs the bulk of
+// step k's trailing update meanwhile.  evP[k]: panels of step k ready;
+// evT[k]: bulk update of step k done.  tc[2]: plans with separate
 // lo/transposed buffers for even and odd steps.
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
@@ -1076,26 +1153,22 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
   cudaEventRecord(fork, st);
   cudaStreamWaitEvent(la, fork, 0);
   diag_and_panels(A, ld, Npad, Dinv, info, 1, 0, la);
-  if (K > 1) tc_split(tc[0], 0, la);
   cudaEventRecord(evP[0], la);
   for (int k = 0; k + 1 < K; ++k) {
     const int rem = Npad - (k + 1) * LU_NB;
     const TcPlan& P = tc[k & 1];
     if (k >= 1) cudaStreamWaitEvent(la, evT[k - 1], 0);
-    int e;
     {
       KScope crit(la, KC_LU_CRIT);
-      e = tc_gemm_sub(P, k, 0, 0, rem, LU_NB, err, la);  // block column k+1
-      if (!e && rem > LU_NB) e = tc_gemm_sub(P, k, 0, LU_NB, LU_NB, rem - LU_NB, err, la);  // block row
-      if (e) return e;
+      thin_update(A, ld, k, rem, la);  // block column and block row k+1
       diag_and_panels(A, ld, Npad, Dinv, info, 1, k + 1, la);
-      if (k + 2 < K) tc_split(tc[(k + 1) & 1], k + 1, la);
     }
     cudaEventRecord(evP[k + 1], la);
     cudaStreamWaitEvent(st, evP[k], 0);
     if (rem > LU_NB) {
       KScope trail(st, KC_LU_TRAIL);
-      e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
+      tc_split(P, k, st);
+      int e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
       if (e) return e;
     }
     cudaEventRecord(evT[k], st);

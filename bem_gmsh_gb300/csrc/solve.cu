@@ -181,12 +181,18 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   double relres = 1.0;
   std::vector<double> H((m + 1) * m), cg(m), sg(m), gvec(m + 1), y(m);
   bool converged = false;
+  double prev_beta = INFINITY;
   while (iters < max_iter && !converged) {
     // r = b - A x (FP64)
     bem::residual64(A64, lda, N, x, b, w, st);
     double beta = std::sqrt(dev_dot(c, w, w, N, hbuf));
     relres = beta / bnorm;
     if (relres <= tol) { converged = true; break; }
+    // stagnation at the FP64 rounding floor (a tol below eps |A| |x| / |b|
+    // cannot be reached): a restart cycle that no longer halves the true
+    // residual ends the refinement
+    if (relres < 1e-10 && beta > 0.5 * prev_beta) break;
+    prev_beta = beta;
     bem::scale_copy64(w, 1.0 / beta, V, N, st);
     std::fill(gvec.begin(), gvec.end(), 0.0);
     gvec[0] = beta;

@@ -221,6 +221,83 @@ def from_cad(name, cad, p, properties, bc_type, bc_value, internal=None, region=
     return dad.contiguous()
 
 
+def from_nodes(name, X, p, properties, bc_type, bc_value) -> BEMdata:
+    """BEMdata whose elements take their geometry from their own p+1
+    collocation nodes `X` (ne, p+1, 2) at the Gauss-Legendre points (no CAD
+    nodes): normals and Jacobians at the nodes come from the nodes' Lagrange
+    interpolant (`tan2normal`, src/Core/Input.jl:584), so the node
+    coordinates are the only geometric parameters (as the adjoint needs)."""
+    X = np.asarray(X, dtype=np.float64)
+    ne = X.shape[0]
+    qsi, wi = gauss_legendre(p + 1)
+    _, D = lagrange_basis(qsi, qsi)
+    dx = np.einsum("qk,ekd->eqd", D, X)
+    J = np.sqrt(dx[..., 0] ** 2 + dx[..., 1] ** 2)
+    t = dx / J[..., None]
+    normal = np.stack([t[..., 1], -t[..., 0]], axis=-1)
+    L = np.abs(J @ wi)
+    n = ne * (p + 1)
+    ndof = properties.ndof
+    bt = np.asarray(bc_type).reshape(-1, ndof)
+    bv = np.asarray(bc_value, dtype=np.float64).reshape(-1, ndof)
+    if bt.shape[0] == ne:
+        bt = np.repeat(bt, p + 1, axis=0)
+        bv = np.repeat(bv, p + 1, axis=0)
+    dad = BEMdata(
+        name=name, p=p, ngeo=0, collocation=X.reshape(n, 2), normal=normal.reshape(n, 2),
+        jacobian=J.reshape(n), elem_length=L, geo=np.zeros((ne, 0, 2)), elem_weight=wi,
+        properties=properties, BC=bt.reshape(-1).astype(np.int32), BV=bv.reshape(-1),
+        region=np.zeros(ne, np.int64))
+    return dad.contiguous()
+
+
+def c4_node_counts(count: int = 512, lo: int = 64, hi: int = 4096, seed: int = 0) -> np.ndarray:
+    """Node counts of the batched uneven workload (config C4): log-uniform in
+    [lo, hi], rounded to multiples of 3 (quadratic elements)."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    return np.maximum(3 * np.round(n / 3).astype(int), 3 * (lo // 3))
+
+
+def c4_domains(sizes, seed0: int = 100, amp: float = 0.1):
+    """Star domains of the batched workload: domain i has sizes[i] nodes and
+    seed seed0 + i (a_k ~ U(0, amp))."""
+    return [star_domain(int(n) // 3, p=2, seed=seed0 + i, amp=amp) for i, n in enumerate(sizes)]
+
+
+def star_adjoint_case(ne: int, p: int = 2, seed: int = 0, amp: float = 0.1, target_amp: float = 0.02):
+    """Shape-gradient case (config C5): star boundary with nodes at the
+    Gauss-Legendre points of each element's angular span, node-interpolant
+    geometry (`from_nodes`), T = e^x cos y with Dirichlet data on theta in
+    [0, pi) and Neumann data on [pi, 2 pi).  The target shape scales the node
+    radii by a smooth seeded factor 1 + target_amp z(theta), z a unit-variance
+    random trigonometric sum of degree <= 3.  Returns (dad, target_dad): the
+    target shares the boundary data arrays, so solving it gives q* on the
+    Dirichlet nodes."""
+    props = Laplace(1.0)
+    r, _ = star_radius(seed, amp)
+    qsi, _ = gauss_legendre(p + 1)
+    th = 2 * np.pi * (np.arange(ne)[:, None] + (qsi[None, :] + 1) / 2) / ne
+    rad = r(th)
+    X = np.stack([rad * np.cos(th), rad * np.sin(th)], axis=-1)
+    start = 2 * np.pi * np.arange(ne) / ne
+    dirichlet = np.repeat(start < np.pi, p + 1)
+    base = from_nodes(f"adj{seed}", X, p, props, np.ones((ne, 1), np.int32), np.zeros((ne, 1)))
+    Xn = base.collocation
+    Tv = np.exp(Xn[:, 0]) * np.cos(Xn[:, 1])
+    gx, gy = Tv, -np.exp(Xn[:, 0]) * np.sin(Xn[:, 1])
+    qv = -(gx * base.normal[:, 0] + gy * base.normal[:, 1])
+    BC = np.where(dirichlet, 0, 1).astype(np.int32)
+    BV = np.where(dirichlet, Tv, qv)
+    dad = from_nodes(f"adj{seed}", X, p, props, BC, BV)
+    rng = np.random.default_rng(10_000 + seed)
+    z = rng.standard_normal(7)
+    zt = (z[0] + sum(z[2 * k - 1] * np.cos(k * th) + z[2 * k] * np.sin(k * th) for k in (1, 2, 3))) / np.sqrt(7.0)
+    Xt = X * (1 + target_amp * zt)[..., None]
+    target = from_nodes(f"adj{seed}_target", Xt, p, props, BC, BV)
+    return dad, target
+
+
 def _segment_cad(a, b, nel, p):
     """CAD nodes of `nel` straight elements from a to b, p+1 equispaced each."""
     a = np.asarray(a, np.float64)

@@ -48,7 +48,7 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms in the background."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms in the background."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -61,7 +61,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -114,10 +114,56 @@ def cpu_reference(dad_factory, steps, warmup, npg):
     return ts, x
 
 
+def extra_configs(ctx):
+    """Config C4 (512 uneven star domains, batched solve) and C5 (adjoint
+    shape gradients of 64 domains x 1023 nodes), wall-clock through the
+    public API with host buffers."""
+    import numpy as np
+    from bem_gmsh_gb300.geometry import c4_node_counts, c4_domains, star_adjoint_case
+    from bem_gmsh_gb300.api import solve_batch, adjoint_laplace, solve
+    out = {}
+    sizes = c4_node_counts(512, seed=0)
+    dads = c4_domains(sizes)
+    solve_batch(dads[:32], npg=16, mode="mixed", nworkers=16, ctx=ctx)  # warm-up (workspaces)
+    t = time.perf_counter()
+    xs, st = solve_batch(dads, npg=16, mode="mixed", nworkers=16, ctx=ctx, return_stats=True)
+    dt = time.perf_counter() - t
+    ent = float(np.sum(sizes.astype(float) ** 2))
+    idx = np.linspace(0, len(dads) - 1, 64).astype(int)
+    sub = [c4_domains([sizes[i]], seed0=100 + int(i))[0] for i in idx]  # same domains, fresh copies
+    t64 = time.perf_counter()
+    xf = solve_batch(sub, npg=16, mode="fp64", nworkers=16, ctx=ctx)
+    dt64 = time.perf_counter() - t64
+    errs = [float(np.linalg.norm(xs[i] - f) / np.linalg.norm(f)) for i, f in zip(idx, xf)]
+    out["batched_c4"] = {
+        "domains": len(dads), "nodes_min": int(sizes.min()), "nodes_max": int(sizes.max()),
+        "sum_entries": ent, "seconds": dt, "solves_per_s": len(dads) / dt, "entries_per_s": ent / dt,
+        "workers": 16, "max_gmres_iterations": int(max(s["iterations"] for s in st)),
+        "fp64_sample": {"domains": len(idx), "seconds": dt64, "max_rel_err": max(errs),
+                        "median_rel_err": float(np.median(errs))},
+        "note": "wall clock through solve_batch with host buffers; per-domain pipelines on 16 worker streams"}
+    cases = [star_adjoint_case(341, p=2, seed=s) for s in range(64)]
+    qts = []
+    for d, tg in cases:
+        solve(tg, npg=16, mode="mixed", ctx=ctx)
+        qts.append(np.where(tg.BC == 0, tg.cache["x"], 0.0))
+    adjoint_laplace(cases[0][0], qts[0], npg=16, ctx=ctx)
+    t = time.perf_counter()
+    res = [adjoint_laplace(d, q, npg=16, ctx=ctx, return_stats=True) for (d, _), q in zip(cases, qts)]
+    dt = time.perf_counter() - t
+    out["adjoint_c5"] = {
+        "domains": len(cases), "nodes": cases[0][0].n, "seconds": dt, "gradients_per_s": len(cases) / dt,
+        "ms_per_gradient": 1e3 * dt / len(cases),
+        "max_iterations_fwd_plus_adj": int(max(r[2]["iterations"] for r in res)),
+        "note": "J and dJ/d(node x, y): forward + adjoint mixed solves and the backward kernels; "
+                "finite-difference checks against the FP64 oracle are in tests/test_gpu_adjoint.py"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ne", type=int, default=2731)
@@ -125,6 +171,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-samples", type=int, default=1)
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched (C4) and adjoint (C5) lines")
     args = ap.parse_args()
     assert args.warmup >= 3 or args.impl == "reference" or args.warmup >= 0
 
@@ -286,9 +333,11 @@ def main():
         # look-ahead column and row block updates (4 128^2 rem) per step
         "lu_crit": ("tensor", sum(4.0 / 3.0 * 128 ** 3 + 8.0 * 128 * 128 * r for r in rems), "TFLOP/s",
                     "latency-bound chain: one diagonal block per step on one SM"),
-        # flops: bulk trailing updates, 2 rem'^2 128 per step (3xTF32 counts once)
-        "lu_trail": ("tensor", sum(2.0 * max(r - 128, 0) ** 2 * 128 for r in rems), "TFLOP/s",
-                     "3xTF32 tcgen05 trailing updates"),
+        # bytes: the bulk trailing update reads and writes its FP32 block once
+        # per step, 8 rem'^2 B (3xTF32 intensity 96 flop/B is below the TF32
+        # machine balance, so HBM bounds it); operands come from L2
+        "lu_trail": ("hbm", sum(8.0 * max(r - 128, 0) ** 2 for r in rems), "GB/s",
+                     "tcgen05 3xTF32 trailing updates (k_gemm_tc): C read + write per step"),
         # bytes: FP32 L and U read once per preconditioner application
         "trsv": ("hbm", 4.0 * nb * nb * iters_last, "GB/s", "FP32 LU read per sweep pair"),
         # bytes: one FP64 A read per product (initial residual + one per iteration + final)
@@ -303,11 +352,22 @@ def main():
         pk = hbm if bound == "hbm" else bf16
         classes[k] = {"bound": bound, "achieved": ach, "unit": unit, "peak": pk, "frac": ach / pk,
                       "ms_per_step": ms_k / args.steps, "note": note}
-    dom = max(classes, key=lambda k: classes[k]["ms_per_step"])
+    # the dominant kernel of the launch list (profiles/) is the tcgen05 GEMM
+    # of the bulk trailing update; its class is lu_trail
+    dom = "lu_trail" if "lu_trail" in classes else max(classes, key=lambda k: classes[k]["ms_per_step"])
     roof = dict(classes[dom])
-    roof.update({"kernel_class": dom, "traffic": None, "peak_source": src,
-                 "peak_note": ("measured dense bf16 burst (TF32 dense is half of it)"
-                               if roof["bound"] == "tensor" else "measured copy bandwidth")})
+    flops_trail = sum(2.0 * max(r - 128, 0) ** 2 * 128 for r in rems)
+    roof.update({"kernel": "k_gemm_tc (bulk trailing update)", "kernel_class": dom,
+                 "traffic": None,
+                 "peak_source": src,
+                 "peak_note": "measured copy bandwidth",
+                 "tensor_view": {"algorithmic_tflops": flops_trail * args.steps / (ktimes["lu_trail"][0] * 1e-3) / 1e12,
+                                 "tf32_mma_tflops": 3 * flops_trail * args.steps / (ktimes["lu_trail"][0] * 1e-3) / 1e12,
+                                 "tf32_dense_peak_tflops": bf16 / 2}})
+
+    extra = {}
+    if not args.no_extra:
+        extra = extra_configs(ctx)
 
     # CPU baseline: the oracle port on the host cores, one full solve sample
     cpu_ts, x_orc = cpu_reference(make, max(1, args.cpu_samples), 0, args.npg)
@@ -338,6 +398,7 @@ def main():
                                        f"{cores} threads + LAPACK LU"},
             "clocks": clk, "gpu_launches": int(launches),
         }
+        line.update(extra)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -213,6 +213,21 @@ int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, int npg, do
                                    void* cuda_stream);
 
 /*
+ * Shape gradient by the adjoint method (no reference counterpart; built on
+ * the path's assembly and solve, src/Core/Assembly_full.jl:61-175 and
+ * src/Core/Boundary_conditions.jl:20-75).  Laplace, elements with their
+ * geometry from their own nodes (geom->ngeo = 0), no internal points.
+ * J = 1/2 sum over nodes with BC = 0 of (q_i - q_target_i)^2, with q from the
+ * mixed-precision solve; grad receives dJ/dx_j, dJ/dy_j (2n, node-major)
+ * with BC, BV and q_target held fixed.  The influence entries are
+ * recomputed in the backward kernels, not stored.  mem says where BC, BV,
+ * q_target, J and grad live (geometry as in the other calls).
+ */
+int bem_adjoint_laplace2d(bem_ctx* ctx, const bem_geom2d* geom, double k, const int32_t* BC, const double* BV,
+                          const double* q_target, int npg, double near_factor, double tol, int max_iter,
+                          int mem, double* J, double* grad, bem_solve_stats* stats);
+
+/*
  * Batched solves of ndom independent domains with uneven sizes (the
  * reference solves one mesh per `solve(dad)` call, src/Core/Solver.jl:24-64;
  * there is no batched counterpart).  Domain d is geoms[d]; its BC/BV entries

@@ -9,15 +9,7 @@ from bem_gmsh_gb300.api import solve, solve_batch
 pytestmark = pytest.mark.gpu
 
 
-def c4_sizes(count, lo=64, hi=4096, seed=0):
-    """Node counts log-uniform in [lo, hi], multiples of 3 (config C4)."""
-    rng = np.random.default_rng(seed)
-    n = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
-    return np.maximum(3 * np.round(n / 3).astype(int), 3 * (lo // 3))
-
-
-def make_batch(sizes, seed0=100):
-    return [star_domain(int(n) // 3, p=2, seed=seed0 + i, amp=0.1) for i, n in enumerate(sizes)]
+from bem_gmsh_gb300.geometry import c4_node_counts as c4_sizes, c4_domains as make_batch
 
 
 def test_batch_matches_single_and_fp64():
