@@ -376,13 +376,15 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
           b_df[s] = df::add(b_df[s], df::mul(gcol ? Hs : Gs, bvv));
           av[s] = df::to_double(gcol ? df::neg(Gs) : Hs);
         }
+        // only far entries are stored: near and on-element entries belong to
+        // the near and singular kernels, which may run concurrently
         double* Ac = (double*)a.H + (size_t)src0 + (size_t)j * ld;
-        if (vec_ok) {
+        if (vec_ok && far[0] && far[1]) {
           *(double2*)Ac = make_double2(av[0], av[1]);
         } else {
 #pragma unroll
           for (int s = 0; s < SPT; ++s)
-            if (src0 + s < a.nt) Ac[s] = av[s];
+            if (far[s] && src0 + s < a.nt) Ac[s] = av[s];
         }
       }
       continue;
@@ -439,10 +441,14 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
           if constexpr (FUSED) bacc[r] += (bcj == 0) ? -(double)hv[b][r] * bvj : (double)gv[b][r] * bvj;
         }
         const size_t row0 = (size_t)src0 * DOF;
+        // only far entries are stored (see the double-float branch)
+        bool allfar = true;
+#pragma unroll
+        for (int s = 0; s < SPT; ++s) allfar = allfar && far[s];
         if constexpr (!FUSED) {
           OutT* Hc = (OutT*)a.H + row0 + (size_t)col * ld;
           OutT* Gc = (OutT*)a.G + row0 + (size_t)col * ldg;
-          if (vec_ok) {
+          if (vec_ok && allfar) {
             typename VecOf<OutT>::type hvv, gvv;
             OutT* hp = (OutT*)&hvv;
             OutT* gp = (OutT*)&gvv;
@@ -453,14 +459,14 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
           } else {
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-              if (src0 + r / DOF < a.nt) { Hc[r] = hv[b][r]; Gc[r] = gv[b][r]; }
+              if (far[r / DOF] && src0 + r / DOF < a.nt) { Hc[r] = hv[b][r]; Gc[r] = gv[b][r]; }
           }
         } else {
           OutT* Ac = (OutT*)a.H + row0 + (size_t)col * ld;
           OutT av[RPT];
 #pragma unroll
           for (int r = 0; r < RPT; ++r) av[r] = (bcj == 0) ? -gv[b][r] : hv[b][r];
-          if (vec_ok) {
+          if (vec_ok && allfar) {
             typename VecOf<OutT>::type v;
             OutT* vp = (OutT*)&v;
 #pragma unroll
@@ -473,7 +479,7 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
           } else {
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-              if (src0 + r / DOF < a.nt) {
+              if (far[r / DOF] && src0 + r / DOF < a.nt) {
                 Ac[r] = av[r];
                 if constexpr (PREC == 2) a.A32[row0 + r + (size_t)col * ld] = (float)av[r];
               }
@@ -552,13 +558,6 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fa.pair_count = q.counters;
   fa.pairs = q.pairs;
   fa.status = q.counters + 1;
-  constexpr int SPT = RPT / DOF;
-  dim3 grid((g.nt + 32 * SPT - 1) / (32 * SPT), (g.ne + 31) / 32);
-  {
-    KScope ks(st, KC_FAR);
-    far_kernel<NC, PREC, FUSED><<<grid, 256, 0, st>>>(fa);
-  }
-
   NearArgs na{};
   na.g = g; na.R = q.R; na.ph = q.ph; na.near_factor = q.near_factor;
   na.ld = q.ld; na.ldg = q.ldg; na.pair_cap = q.pair_cap;
@@ -571,9 +570,29 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fi.nt = g.nt; fi.n = g.n; fi.ld = q.ld; fi.H = q.H; fi.A32 = q.A32;
   fi.bc = q.bc; fi.bv = q.bv; fi.b = q.b; fi.rowsum = q.rowsum; fi.gdiag = q.gdiag;
   fi.mode = na.mode;
+
+  // the on-element rows need neither the far results nor the pair list: on
+  // a side stream they run beside the far and near kernels (every kernel
+  // writes its own entries; row sums are atomic)
+  const bool side = q.aux != nullptr && g.n > 0;
+  if (side) {
+    cudaEventRecord(q.ev_fork, st);
+    cudaStreamWaitEvent(q.aux, q.ev_fork, 0);
+    launch_singular(na, NC, g.n, q.aux);
+    cudaEventRecord(q.ev_join, q.aux);
+  }
+  constexpr int SPT = RPT / DOF;
+  dim3 grid((g.nt + 32 * SPT - 1) / (32 * SPT), (g.ne + 31) / 32);
+  {
+    KScope ks(st, KC_FAR);
+    far_kernel<NC, PREC, FUSED><<<grid, 256, 0, st>>>(fa);
+  }
   {
     KScope ks(st, KC_NEAR);
-    launch_near(na, fi, NC, g.nt, g.n, st);
+    launch_near_pairs(na, NC, st);
+    if (!side) launch_singular(na, NC, g.n, st);
+    if (side) cudaStreamWaitEvent(st, q.ev_join, 0);
+    launch_finalize(fi, NC, g.nt, st);
   }
   count_launches(g.n > 0 ? 8 : 7);
 }

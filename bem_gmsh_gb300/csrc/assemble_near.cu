@@ -190,19 +190,23 @@ __global__ void finalize_kernel(FinalArgs a) {
 
 
 
-void launch_near(const NearArgs& na, const FinalArgs& fi, int nc, int nt, int n, cudaStream_t st) {
+void launch_near_pairs(const NearArgs& na, int nc, cudaStream_t st) {
   int nblk = (na.pair_cap + 127) / 128;
   if (nblk > 152 * 16) nblk = 152 * 16;
   if (nblk < 1) nblk = 1;
-  if (nc == 1) {
-    near_kernel<1><<<nblk, 128, 0, st>>>(na);
-    if (n > 0) singular_kernel<1><<<(n + 63) / 64, 64, 0, st>>>(na);
-    finalize_kernel<1><<<(nt + 255) / 256, 256, 0, st>>>(fi);
-  } else {
-    near_kernel<4><<<nblk, 128, 0, st>>>(na);
-    if (n > 0) singular_kernel<4><<<(n + 63) / 64, 64, 0, st>>>(na);
-    finalize_kernel<4><<<(nt + 255) / 256, 256, 0, st>>>(fi);
-  }
+  if (nc == 1) near_kernel<1><<<nblk, 128, 0, st>>>(na);
+  else near_kernel<4><<<nblk, 128, 0, st>>>(na);
+}
+
+void launch_singular(const NearArgs& na, int nc, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  if (nc == 1) singular_kernel<1><<<(n + 63) / 64, 64, 0, st>>>(na);
+  else singular_kernel<4><<<(n + 63) / 64, 64, 0, st>>>(na);
+}
+
+void launch_finalize(const FinalArgs& fi, int nc, int nt, cudaStream_t st) {
+  if (nc == 1) finalize_kernel<1><<<(nt + 255) / 256, 256, 0, st>>>(fi);
+  else finalize_kernel<4><<<(nt + 255) / 256, 256, 0, st>>>(fi);
 }
 
 }  // namespace bem

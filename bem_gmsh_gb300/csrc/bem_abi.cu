@@ -190,6 +190,9 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
     if (b.p) cudaFree(b.p);
   c->prof.release();
   for (auto e : c->events) cudaEventDestroy(e);
+  if (c->asm_fork) cudaEventDestroy(c->asm_fork);
+  if (c->asm_join) cudaEventDestroy(c->asm_join);
+  if (c->asm_stream) cudaStreamDestroy(c->asm_stream);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -291,6 +294,17 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
   q.counters = (int*)c->get(bem_ctx::SLOT_COUNTERS, 64);
   q.absmax = (unsigned long long*)((char*)q.counters + 32);
   if (!q.rows || !q.nodes || !q.elems || !q.rowsum || !q.gdiag || !q.counters) return BEM_ERR_NOMEM;
+  if (!c->asm_stream) {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&c->asm_stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->asm_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->asm_join, cudaEventDisableTiming) != cudaSuccess)
+      return c->cuda_fail(cudaGetLastError(), "assembly side stream");
+  }
+  q.aux = c->asm_stream;
+  q.ev_fork = c->asm_fork;
+  q.ev_join = c->asm_join;
   if (q.prec == 3) {
     q.nodes_df = (bem::NodeDF*)c->get(bem_ctx::SLOT_NODES_DF, sizeof(bem::NodeDF) * (size_t)q.g.n);
     q.logtab = (float4*)c->get(bem_ctx::SLOT_LOGTAB, sizeof(float4) * 136);

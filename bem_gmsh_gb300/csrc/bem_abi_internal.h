@@ -34,6 +34,9 @@ struct bem_ctx {
   int opt_far_df = 1;   // BEM_OPT_FAR_DF
   void* cusolver_handle = nullptr;  // FP64 comparison path (created on first use)
   std::vector<bem_ctx*> workers;    // sub-contexts of batched calls (own streams)
+  // side stream and events of the assembly (created on first use)
+  cudaStream_t asm_stream = nullptr;
+  cudaEvent_t asm_fork = nullptr, asm_join = nullptr;
   bem::KProf prof;      // BEM_OPT_KERNEL_TIMING
 
   // second stream and events of the lookahead LU (created on first use)

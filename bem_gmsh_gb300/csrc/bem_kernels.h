@@ -87,7 +87,10 @@ struct FinalArgs {
   int mode;
 };
 
-void launch_near(const NearArgs& na, const FinalArgs& fi, int nc, int nt, int n, cudaStream_t st);
+// near pairs (listed by the far kernel), on-element rows, row-sum diagonal
+void launch_near_pairs(const NearArgs& na, int nc, cudaStream_t st);
+void launch_singular(const NearArgs& na, int nc, int n, cudaStream_t st);
+void launch_finalize(const FinalArgs& fi, int nc, int nt, cudaStream_t st);
 
 // One assembly request; all pointers are device pointers.
 struct AsmRequest {
@@ -118,6 +121,10 @@ struct AsmRequest {
   int2* pairs;
   int pair_cap;
   unsigned long long* absmax;  // scratch: largest |coordinate|
+  // optional side stream for the on-element kernel (runs beside the far and
+  // near kernels; joined before the diagonal), with its fork/join events
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 // Launch the whole assembly on `stream` (asynchronous).  Returns 0 or a

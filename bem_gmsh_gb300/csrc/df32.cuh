@@ -81,6 +81,10 @@ DF_HD double dfrom(uint64_t u) {
 #endif
 }
 
+// exact float of a small integer (|i| < 2^22) with one FP32 add (keeps the
+// int-to-float conversion off the FP64/conversion pipe)
+DF_HD float small_int_to_float(int i) { return sub_(ffrom(0x4B400000u + (uint32_t)i), 12582912.0f); }
+
 // s + e == a + b exactly
 DF_HD f2 two_sum(float a, float b) {
   const float s = add_(a, b);
@@ -194,7 +198,7 @@ DF_HD f2 log(f2 x, const LogEntry* tab) {
   const int i = (int)((ih >> 15) & 0xffu);                             // top 8 fraction bits
   const int ic = (i + 1) >> 1;                                         // nearest centre
   const LogEntry T = tab[ic];
-  const float c = add_(1.0f, mul_((float)ic, 0.0078125f));
+  const float c = add_(1.0f, mul_(small_int_to_float(ic), 0.0078125f));
   const float f = sub_(m, c);                                          // exact, |f| <= 2^-8
   // u = (f + x.l 2^-E) / c
   f2 u = two_prod(f, T.rc_h);
@@ -214,18 +218,23 @@ DF_HD f2 log(f2 x, const LogEntry* tab) {
   // E log 2 + log c
   const float ln2_h = 0.693147182464599609375f;          // 0x3f317218
   const float ln2_l = -1.9046542121259336e-09f;          // log 2 - ln2_h
-  f2 el = two_prod((float)E, ln2_h);
-  el.l = fma_((float)E, ln2_l, el.l);
+  const float Ef = small_int_to_float(E);
+  f2 el = two_prod(Ef, ln2_h);
+  el.l = fma_(Ef, ln2_l, el.l);
   el = fast_two_sum(el.h, el.l);
   return add(add(el, f2{T.lc_h, T.lc_l}), l1);
 }
 
-// nearest double of h + l built with integer operations (no FP64 pipe);
-// zero, subnormal and non-finite leading parts take the plain conversion
+// nearest double of h + l built with integer operations only (no FP64 or
+// conversion pipe); a zero or subnormal leading part gives a signed zero
+// (far-field entries are many orders above 2^-126), infinities and NaNs
+// keep their class
 DF_HD double to_double(f2 a) {
   const uint32_t ih = fbits(a.h);
   const uint32_t eh = (ih >> 23) & 0xffu;
-  if (eh == 0u || eh == 255u) return (double)a.h + (double)a.l;
+  if (eh == 0u) return dfrom((uint64_t)(ih & 0x80000000u) << 32);
+  if (eh == 255u)
+    return dfrom(((uint64_t)(ih & 0x80000000u) << 32) | 0x7FF0000000000000ull | ((uint64_t)(ih & 0x7fffffu) << 29));
   uint64_t D = ((uint64_t)(ih & 0x80000000u) << 32) | ((uint64_t)(eh + 896u) << 52) |
                ((uint64_t)(ih & 0x7fffffu) << 29);
   const uint32_t il = fbits(a.l);

@@ -95,6 +95,13 @@ def test_to_double_rounding(h):
     h.df_to_double_batch(hi.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
                          lo.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), x.size, _p(out))
     exact = hi.astype(np.longdouble) + lo.astype(np.longdouble)
+    # zero and non-finite leading parts
+    z = np.zeros(4, np.float32)
+    hz = np.array([0.0, -0.0, np.inf, -np.inf], np.float32)
+    oz = np.empty(4)
+    h.df_to_double_batch(hz.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                         z.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 4, _p(oz))
+    assert oz[0] == 0.0 and oz[1] == 0.0 and np.signbit(oz[1]) and oz[2] == np.inf and oz[3] == -np.inf
     # within one double ulp of the exact sum (round half away at the last bit)
     ulp = np.spacing(np.abs(out))
     assert np.all(np.abs(out.astype(np.longdouble) - exact) <= ulp.astype(np.longdouble))
