@@ -19,10 +19,11 @@ struct TcPlan;
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
               const TcPlan* tc = nullptr, int* err = nullptr);
 // out <- U^{-1} L^{-1} r on padded FP32 vectors.  tmp: Npad floats (the
-// forward result), flags: 2 Npad/LU_NB ints, err: timeout flag.  r may be
-// clobbered.  Returns 0 or a CUDA error code.
+// forward result); tags: 2 Npad words of (epoch, value) scratch, zeroed
+// before the first call; epoch: > 0 and different in every call on the same
+// tags; err: timeout flag.  r may be clobbered.  Returns 0 or a CUDA error.
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
-                 float* out, int* flags, int* err, cudaStream_t st);
+                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st);
 
 void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
                 cudaStream_t st);

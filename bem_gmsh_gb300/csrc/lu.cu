@@ -432,6 +432,14 @@ __global__ void k_panel_gemv(const float* __restrict__ P, int64_t ld, int rows,
 // timeout is reported through `err` instead of hanging.  The launch is
 // cooperative so that all CTAs are resident.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -444,11 +452,11 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 template <bool UPPER>
 __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, int64_t ld, int K,
                                                    const float* __restrict__ Dinv, const float* r,
-                                                   float* y, int* flags, int epoch, int* err) {
+                                                   float* y, unsigned long long* tags, int epoch, int* err) {
   extern __shared__ float Ds[];  // the block's inverse, [col][row], LU_NB * (LU_NB + 1)
   __shared__ float ys[LU_NB];
   __shared__ float part[2][LU_NB];
-  __shared__ int ok;
+  __shared__ int bad;
   const int t = threadIdx.x, row = t & (LU_NB - 1), half = t >> 7;
   const int b = UPPER ? (K - 1 - (int)blockIdx.x) : (int)blockIdx.x;
   const size_t rb = (size_t)b * LU_NB;
@@ -457,9 +465,10 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     int rr = idx & (LU_NB - 1), c = idx >> 7;
     Ds[c * (LU_NB + 1) + rr] = Db[rr + (size_t)c * LU_NB];
   }
-  if (t == 0) ok = 1;
+  if (t == 0) bad = 0;
   float acc = (half == 0) ? r[rb + row] : 0.f;
   const int nj = UPPER ? (K - 1 - b) : b;
+  __syncthreads();
   for (int s = 0; s < nj; ++s) {
     const int j = UPPER ? (K - 1 - s) : s;
     // prefetch this thread's 64 coefficients of block (b, j) before waiting
@@ -467,17 +476,26 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     const float* P = A + (rb + row) + ((size_t)j * LU_NB + half * (LU_NB / 2)) * ld;
 #pragma unroll
     for (int q = 0; q < LU_NB / 2; ++q) pre[q] = P[(size_t)q * ld];
-    if (t == 0) {
+    // y_j arrives as (epoch, value) words: each thread waits for its own
+    if (t < LU_NB) {
+      const unsigned long long* w = tags + (size_t)j * LU_NB + t;
+      unsigned long long v = ld_acquire_u64(w);
       int it = 0;
-      while (ld_acquire(flags + j) != epoch) {
-        if (++it > (1 << 20)) { ok = 0; atomicExch(err, 1); break; }
-        __nanosleep(64);
+      while ((int)(v >> 32) != epoch) {
+        if (++it > (1 << 20)) {
+          bad = 1;
+          break;
+        }
+        if (it > 8) __nanosleep(32);
+        v = ld_acquire_u64(w);
       }
+      ys[t] = __uint_as_float((uint32_t)v);
     }
     __syncthreads();
-    if (!ok) return;
-    if (t < LU_NB) ys[t] = __ldcg(y + (size_t)j * LU_NB + t);
-    __syncthreads();
+    if (bad) {
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
 #pragma unroll
     for (int q = 0; q < LU_NB / 2; ++q) acc -= pre[q] * ys[half * (LU_NB / 2) + q];
     __syncthreads();
@@ -492,10 +510,11 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
   for (int q = half * (LU_NB / 2); q < (half + 1) * (LU_NB / 2); ++q) o += Ds[q * (LU_NB + 1) + row] * ys[q];
   part[half][row] = o;
   __syncthreads();
-  if (t < LU_NB) y[rb + t] = part[0][t] + part[1][t];
-  __threadfence();
-  __syncthreads();
-  if (t == 0) st_release(flags + b, epoch);
+  if (t < LU_NB) {
+    const float v = part[0][t] + part[1][t];
+    y[rb + t] = v;
+    st_relaxed_u64(tags + rb + t, ((unsigned long long)(unsigned)epoch << 32) | __float_as_uint(v));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,7 +1225,7 @@ static void lu_solve_vec_steps(const float* A, int64_t ld, int Npad, const float
 // y = (L U)^{-1} r on a padded FP32 vector.  r is overwritten with the
 // forward result; the solution lands in `out`.  flags: 2K ints of scratch.
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
-                 float* out, int* flags, int* err, cudaStream_t st) {
+                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st) {
   const int K = Npad / LU_NB;
   static int max_coresident = 0;
   static std::once_flag once;
@@ -1228,23 +1247,19 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
   }
   KScope ks(st, KC_TRSV);
   count_launches(2);
-  cudaMemsetAsync(flags, 0, sizeof(int) * 2 * K, st);
-  int epoch = 1;
-  int* f0 = flags;
-  int* f1 = flags + K;
-  float* yfwd = r;  // forward result written in place (blocks only read their own r_b before)
+  unsigned long long* t0 = tags;
+  unsigned long long* t1 = tags + Npad;
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&r, (void*)&tmp,
-                    (void*)&f0, (void*)&epoch, (void*)&err};
+                    (void*)&t0, (void*)&epoch, (void*)&err};
     // forward: r -> tmp (separate output so that no CTA reads a block another rewrote)
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, dim3(K), dim3(256), args,
                                                 dsm, st);
     if (e != cudaSuccess) return (int)e;
   }
-  (void)yfwd;
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&tmp, (void*)&out,
-                    (void*)&f1, (void*)&epoch, (void*)&err};
+                    (void*)&t1, (void*)&epoch, (void*)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, dim3(K), dim3(256), args,
                                                 dsm, st);
     if (e != cudaSuccess) return (int)e;

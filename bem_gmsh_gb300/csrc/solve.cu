@@ -116,13 +116,17 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   double* Z = (double*)c->get(bem_ctx::SLOT_LU4, sizeof(double) * (size_t)N * m);
   double* w = (double*)c->get(bem_ctx::SLOT_LU5, sizeof(double) * ((size_t)N + 64));
   float* rf = (float*)c->get(bem_ctx::SLOT_LU6, sizeof(float) * (3 * (size_t)Npad + 64) +
-                                                   sizeof(int) * (2 * (size_t)K + 64));
+                                                   sizeof(unsigned long long) * (2 * (size_t)Npad));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
   if (!A32 || !cs || !Dinv || !V || !Z || !w || !rf || !info) return BEM_ERR_NOMEM;
   double* hbuf = w + N;  // 64 doubles of scratch
   float* tmpf = rf + Npad;
   float* outf = rf + 2 * (size_t)Npad;
-  int* flags = (int*)(rf + 3 * (size_t)Npad + 64);
+  // (epoch, value) words of the triangular sweeps; zeroed once per solve,
+  // every preconditioner application uses the next epoch
+  unsigned long long* tags = (unsigned long long*)(rf + 3 * (size_t)Npad + 64);
+  cudaMemsetAsync(tags, 0, sizeof(unsigned long long) * 2 * (size_t)Npad, c->stream);
+  int epoch = 0;
   int* werr = info + 1;
   Timer tf, tr;
   bem::TcPlan tcp[2];
@@ -165,7 +169,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   int prc = 0;
   auto precond = [&](const double* v, double* z) {
     bem::to_f32(v, N, Npad, rf, st);
-    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, rf, tmpf, outf, flags, werr, st);
+    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, rf, tmpf, outf, tags, ++epoch, werr, st);
     if (e2) prc = e2;
     bem::from_f32_scale(outf, cs, N, z, st);
   };
