@@ -206,36 +206,52 @@ __global__ void __launch_bounds__(256, 1) k_gemm_tc(const __grid_constant__ CUte
     mma_commit(done);
   }
   __syncwarp();
-  // epilogue: all four warps; the go/no-go decision is block-uniform
+  // epilogue: 8 warps; warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows)
+  // and the column half w / 4.  C is software-pipelined: the first 32 values
+  // are loaded while the MMAs still run, and each block's loads are issued
+  // before the previous block is processed.
+  const int quad = warp & 3, half = warp >> 2;
+  const int row = m0 + quad * 32 + lane;
+  const bool rowok = row < a.M;
+  const bool useC = a.beta != 0.f;
+  float* Crow = a.C + row;
+  const int cb0 = half * (BN / 2);
+  float cnext[32];
+  if (rowok && useC) {
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int col = n0 + cb0 + q;
+      cnext[q] = (col < a.N) ? __ldcs(Crow + (size_t)col * a.ldc) : 0.f;
+    }
+  }
+  // the go/no-go decision is block-uniform
   const bool got = mbar_wait(done, 0);
   const int all_ok = __syncthreads_and(got ? 1 : 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int fail = *((volatile int*)s_fail);
   if (all_ok && !fail) {
-    // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (its rows) and the
-    // column half w / 4; 32 C values are loaded before any is stored
-    const int quad = warp & 3, half = warp >> 2;
-    const int row = m0 + quad * 32 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
-    float* Crow = a.C + row;
-    for (int cb = half * (BN / 2); cb < (half + 1) * (BN / 2); cb += 32) {
+#pragma unroll 1
+    for (int cb = cb0; cb < cb0 + BN / 2; cb += 32) {
+      float cv[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) cv[q] = cnext[q];
+      if (rowok && useC && cb + 32 < cb0 + BN / 2) {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int col = n0 + cb + 32 + q;
+          cnext[q] = (col < a.N) ? __ldcs(Crow + (size_t)col * a.ldc) : 0.f;
+        }
+      }
       uint32_t v[32];
       tmem_ld32(lane_addr + cb, v);
-      if (row < a.M) {
-        float cv[32];
-        if (a.beta != 0.f) {
-#pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const int col = n0 + cb + q;
-            cv[q] = (col < a.N) ? __ldcs(Crow + (size_t)col * a.ldc) : 0.f;
-          }
-        }
+      if (rowok) {
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
           const int col = n0 + cb + q;
           if (col < a.N) {
             const float accv = __uint_as_float(v[q]);
-            const float r = (a.beta == 0.f) ? a.alpha * accv : a.beta * cv[q] + a.alpha * accv;
+            const float r = useC ? a.beta * cv[q] + a.alpha * accv : a.alpha * accv;
             __stcs(Crow + (size_t)col * a.ldc, r);
           }
         }

@@ -114,6 +114,14 @@ def cpu_reference(dad_factory, steps, warmup, npg):
     return ts, x
 
 
+# DRAM traffic of one bulk trailing update (k_gemm_tc) at full C2 size, from
+# profiles/k_gemm_tc_bulk_update_c2_traffic.md: LU step 10 (trailing block
+# 6784^2), dram__bytes_read 198152192 B + dram__bytes_write 123085824 B for
+# 8 * 6784^2 = 368181248 algorithmic bytes.
+GEMM_TRAFFIC_CAPTURE = {"launch": "LU step 10 (trailing block 6784^2)", "read_bytes": 198152192,
+                        "write_bytes": 123085824, "algorithmic_bytes": 8 * 6784 ** 2}
+
+
 def extra_configs(ctx):
     """Config C4 (512 uneven star domains, batched solve) and C5 (adjoint
     shape gradients of 64 domains x 1023 nodes), wall-clock through the
@@ -357,8 +365,15 @@ def main():
     dom = "lu_trail" if "lu_trail" in classes else max(classes, key=lambda k: classes[k]["ms_per_step"])
     roof = dict(classes[dom])
     flops_trail = sum(2.0 * max(r - 128, 0) ** 2 * 128 for r in rems)
+    cap = GEMM_TRAFFIC_CAPTURE
+    ratio = (cap["read_bytes"] + cap["write_bytes"]) / cap["algorithmic_bytes"]
+    nbulk = max(1, sum(1 for r in rems if r > 128))
     roof.update({"kernel": "k_gemm_tc (bulk trailing update)", "kernel_class": dom,
-                 "traffic": None,
+                 "traffic": ratio * algo["lu_trail"][1] / nbulk,
+                 "traffic_note": "bytes per average bulk launch: the measured DRAM read+write / algorithmic "
+                                 "ratio of one full-size ncu capture (%s, %.3f) times the algorithmic bytes "
+                                 "of the average launch; writes still in L2 at kernel end are not counted"
+                                 % (cap["launch"], ratio),
                  "peak_source": src,
                  "peak_note": "measured copy bandwidth",
                  "tensor_view": {"algorithmic_tflops": flops_trail * args.steps / (ktimes["lu_trail"][0] * 1e-3) / 1e12,
