@@ -375,3 +375,51 @@ def adjoint_laplace(dad: BEMdata, q_target, npg: int = 16, near_factor: float = 
         return out + (dict(status=st.status, iterations=st.iterations, t_assemble_ms=st.t_assemble_ms,
                            t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms),)
     return out
+
+
+RBF_KINDS = {"PHS1": 1, "PHS2": 2, "PHS3": 3, "PHS4": 4, "PHS5": 5, "PHS6": 6, "PHS7": 7, "fundamental": 10}
+
+
+def discretize(cad, p: int, ctx: _lib.Context | None = None):
+    """Collocation nodes (ne, p+1, 2), outward normals, Jacobians (ne, p+1),
+    element lengths (ne,) and Gauss weights (p+1,) of elements given by their
+    equispaced CAD nodes `cad` (ne, ngeo, 2), computed on the device: the
+    geometry loop of `format2d` (src/Core/Input.jl:163-185).  Same outputs as
+    `geometry.discretize_curves`; pass it as `from_cad(..., discretize=...)`."""
+    ctx = ctx or _lib.default_context()
+    cad = np.asarray(cad, dtype=np.float64)
+    ne, ngeo = cad.shape[0], cad.shape[1]
+    cx, cy = np.ascontiguousarray(cad[..., 0]), np.ascontiguousarray(cad[..., 1])
+    n = ne * (p + 1)
+    px, py, nx, ny, J = (np.empty(n) for _ in range(5))
+    L = np.empty(ne)
+    wi = np.empty(p + 1)
+    rc = ctx.L.bem_discretize2d(ctx.h, ne, ngeo, p, _ptr(cx), _ptr(cy), _lib.BEM_MEM_HOST, _ptr(px), _ptr(py),
+                                _ptr(nx), _ptr(ny), _ptr(J), _ptr(L), _ptr(wi))
+    ctx.check(rc, "discretize")
+    nodes = np.stack([px, py], axis=-1).reshape(ne, p + 1, 2)
+    normal = np.stack([nx, ny], axis=-1).reshape(ne, p + 1, 2)
+    return nodes, normal, J.reshape(ne, p + 1), L, wi
+
+
+def dibem_fd(dad: BEMdata, rbf: str = "PHS3", dtype=np.float64, epsa: float = 1e-16,
+             ctx: _lib.Context | None = None):
+    """Dense pairwise DIBEM matrices over all collocation points
+    (`_dibem_FD_ka`, src/Laplace/DIBEM_GPU.jl:179-208; Kelvin
+    src/Elasticity/Assembly_GPU.jl:258-280): F_ij = phi(R), D_ij = u*(x_i, x_j)."""
+    ctx = ctx or _lib.default_context()
+    pr = dad.properties
+    kind = 0 if isinstance(pr, Laplace) else 1
+    p0 = float(pr.k) if kind == 0 else float(pr.mu)
+    p1 = 0.0 if kind == 0 else float(pr.nu_eff)
+    pts = np.asarray(dad.collocation, np.float64)
+    px, py = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+    nt = len(pts)
+    dof = 1 if kind == 0 else 2
+    F = np.zeros((nt, nt), dtype=dtype, order="F")
+    D = np.zeros((dof * nt, dof * nt), dtype=dtype, order="F")
+    dt = _lib.BEM_F64 if dtype == np.float64 else _lib.BEM_F32
+    rc = ctx.L.bem_dibem_fd2d(ctx.h, nt, _ptr(px), _ptr(py), kind, p0, p1, RBF_KINDS[rbf], float(epsa), dt,
+                              _lib.BEM_MEM_HOST, _ptr(F), nt, _ptr(D), dof * nt)
+    ctx.check(rc, "dibem_fd")
+    return F, D

@@ -112,6 +112,10 @@ void build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) 
 
 }  // namespace
 
+namespace bem {
+void gauss_legendre_nodes(int n, double* x, double* w) { gauss_legendre(n, x, w); }
+}  // namespace bem
+
 void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) {
   build_rules(g, npg, ew_host, R);
 }

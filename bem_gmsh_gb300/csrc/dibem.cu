@@ -1,0 +1,185 @@
+// Dense pairwise matrices of the dual-interpolation BEM (DIBEM): for every
+// pair of collocation points i != j with R = |x_j - x_i|,
+//   F_ij = phi(R)                      radial basis function
+//   D_ij = u*(x_i, x_j)                fundamental solution
+// restating `_dibem_FD_kernel!` (src/Laplace/DIBEM_GPU.jl:194-208, Laplace:
+// D = -log(R)/(2 pi k)) and `_elast_dibem_FD_kernel!`
+// (src/Elasticity/Assembly_GPU.jl:258-280, Kelvin: D holds the 2x2 block
+// U(r) of `_kelvin2d_UT`).  phi: `_dibem_phi` (DIBEM_GPU.jl:116-139), kinds
+// 1-7 the polyharmonic splines R, R^2 log(R+e), R^3, R^4 log(R+e), R^5,
+// R^6 log(R+e), R^7, kind 10 the fundamental solution.  Entries with
+// i == j or R^2 <= eps^2 stay zero.  Outputs column-major (Julia layout).
+// Each thread writes 16 bytes of one column (2 FP64 or 4 FP32 rows), so a
+// warp stores a contiguous 512-byte segment: the kernel is bound by the HBM
+// write of F and D.
+#include <cfloat>
+#include <cmath>
+
+#include "bem_abi_internal.h"
+
+namespace bem {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T dibem_phi(int kind, T R, T kcond, T epsa) {
+  const T R2 = R * R;
+  switch (kind) {
+    case 1: return R;
+    case 2: return R2 * log(R + epsa);
+    case 3: return R2 * R;
+    case 4: return (R2 * R2) * log(R + epsa);
+    case 5: return R2 * R2 * R;
+    case 6: return (R2 * R2 * R2) * log(R + epsa);
+    case 7: return R2 * R2 * R2 * R;
+    default: return -log(R) / (T(2) * T(3.14159265358979323846) * kcond);
+  }
+}
+
+// Laplace: F, D (nt x nt)
+template <typename T>
+__global__ void dibem_laplace_kernel(int nt, const double* __restrict__ px, const double* __restrict__ py,
+                                     T kcond, int kind, T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
+  constexpr int RPT = 16 / sizeof(T);
+  const int j = blockIdx.y;
+  const int i0 = (blockIdx.x * blockDim.x + threadIdx.x) * RPT;
+  if (i0 >= nt) return;
+  const T xj = (T)px[j], yj = (T)py[j];
+  const T inv2pi = T(1) / (T(2) * T(3.14159265358979323846));
+  T f[RPT], d[RPT];
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int i = i0 + r;
+    f[r] = T(0);
+    d[r] = T(0);
+    if (i < nt && i != j) {
+      const T rx = xj - (T)px[i], ry = yj - (T)py[i];
+      const T R2 = rx * rx + ry * ry;
+      if (R2 > eps2) {
+        const T R = sqrt(R2);
+        d[r] = -log(R) * inv2pi / kcond;
+        f[r] = dibem_phi<T>(kind, R, kcond, epsa);
+      }
+    }
+  }
+  T* Fc = F + i0 + (size_t)j * ldf;
+  T* Dc = D + i0 + (size_t)j * ldd;
+  const bool vec = (i0 + RPT <= nt) && ((ldf | ldd) % RPT == 0) && (((uintptr_t)F | (uintptr_t)D) % 16 == 0);
+  if (vec) {
+    if constexpr (sizeof(T) == 8) {
+      *(double2*)Fc = make_double2(f[0], f[1]);
+      *(double2*)Dc = make_double2(d[0], d[1]);
+    } else {
+      *(float4*)Fc = make_float4(f[0], f[1], f[2], f[3]);
+      *(float4*)Dc = make_float4(d[0], d[1], d[2], d[3]);
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+      if (i0 + r < nt) {
+        Fc[r] = f[r];
+        Dc[r] = d[r];
+      }
+  }
+}
+
+// Kelvin: F (nt x nt), D (2nt x 2nt, node-major 2x2 blocks u11 u12; u12 u22)
+template <typename T>
+__global__ void dibem_kelvin_kernel(int nt, const double* __restrict__ px, const double* __restrict__ py,
+                                    T mu, T nu, int kind, T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
+  const int j = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  T f = T(0), u11 = T(0), u12 = T(0), u22 = T(0);
+  if (i != j) {
+    const T rx = (T)px[j] - (T)px[i], ry = (T)py[j] - (T)py[i];
+    const T R2 = rx * rx + ry * ry;
+    if (R2 > eps2) {
+      const T R = sqrt(R2);
+      f = dibem_phi<T>(kind, R, T(1), epsa);
+      // U of the 2-D Kelvin solution (`_kelvin2d_UT`, Elasticity/Fundamental.jl)
+      const T pi = T(3.14159265358979323846);
+      const T dr1 = rx / R, dr2 = ry / R;
+      const T prod1 = T(4) * pi * (T(1) - nu);
+      const T prod2 = (T(3) - T(4) * nu) * (-log(R));
+      const T base = T(2) * prod1 * mu;
+      u11 = (prod2 + dr1 * dr1) / base;
+      u12 = (dr1 * dr2) / base;
+      u22 = (prod2 + dr2 * dr2) / base;
+    }
+  }
+  F[i + (size_t)j * ldf] = f;
+  T* c0 = D + 2 * (size_t)i + (size_t)(2 * j) * ldd;
+  T* c1 = c0 + ldd;
+  c0[0] = u11;
+  c0[1] = u12;
+  c1[0] = u12;
+  c1[1] = u22;
+}
+
+}  // namespace
+}  // namespace bem
+
+using namespace bem;
+
+extern "C" int bem_dibem_fd2d(bem_ctx* c, int nt, const double* px, const double* py, int kind, double prm0,
+                              double prm1, int rbf, double epsa, int dtype, int mem, void* F, int64_t ldf,
+                              void* D, int64_t ldd) {
+  if (!c || nt <= 0 || !px || !py || !F || !D) return BEM_ERR_INVALID;
+  if (kind != 0 && kind != 1) return BEM_ERR_INVALID;
+  if (!((rbf >= 1 && rbf <= 7) || rbf == 10)) return BEM_ERR_INVALID;
+  if (dtype != BEM_F32 && dtype != BEM_F64) return BEM_ERR_INVALID;
+  if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  const int dof = kind == 0 ? 1 : 2;
+  if (ldf < nt || ldd < (int64_t)dof * nt) return BEM_ERR_INVALID;
+  if (kind == 0 && !(prm0 > 0)) return BEM_ERR_INVALID;
+  if (kind == 1 && (!(prm0 > 0) || !(prm1 < 0.5) || !(prm1 > -1.0))) return BEM_ERR_INVALID;
+  CallScope cs(c);
+  cudaSetDevice(c->device);
+  const size_t esz = dtype == BEM_F32 ? 4 : 8;
+  const size_t n = (size_t)nt;
+  const double *dx = px, *dy = py;
+  void *dF = F, *dD = D;
+  int64_t lf = ldf, lD = ldd;
+  if (mem == BEM_MEM_HOST) {
+    double* g = (double*)c->get(bem_ctx::SLOT_GEOM, sizeof(double) * 2 * n);
+    lf = (int64_t)((n + 3) / 4 * 4);
+    lD = (int64_t)((dof * n + 3) / 4 * 4);
+    void* o0 = c->get(bem_ctx::SLOT_OUT0, esz * (size_t)lf * n);
+    void* o1 = c->get(bem_ctx::SLOT_OUT1, esz * (size_t)lD * dof * n);
+    if (!g || !o0 || !o1) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(g, px, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(g + n, py, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    dx = g;
+    dy = g + n;
+    dF = o0;
+    dD = o1;
+  }
+  if (kind == 0) {
+    const int rpt = (int)(16 / esz);
+    dim3 grid((unsigned)((n + 128 * rpt - 1) / (128 * rpt)), (unsigned)n);
+    if (dtype == BEM_F64)
+      dibem_laplace_kernel<double><<<grid, 128, 0, c->stream>>>(nt, dx, dy, prm0, rbf, epsa, DBL_EPSILON * DBL_EPSILON,
+                                                               (double*)dF, lf, (double*)dD, lD);
+    else
+      dibem_laplace_kernel<float><<<grid, 128, 0, c->stream>>>(nt, dx, dy, (float)prm0, rbf, (float)epsa,
+                                                              FLT_EPSILON * FLT_EPSILON, (float*)dF, lf, (float*)dD, lD);
+  } else {
+    dim3 grid((unsigned)((n + 127) / 128), (unsigned)n);
+    if (dtype == BEM_F64)
+      dibem_kelvin_kernel<double><<<grid, 128, 0, c->stream>>>(nt, dx, dy, prm0, prm1, rbf, epsa,
+                                                              DBL_EPSILON * DBL_EPSILON, (double*)dF, lf, (double*)dD, lD);
+    else
+      dibem_kelvin_kernel<float><<<grid, 128, 0, c->stream>>>(nt, dx, dy, (float)prm0, (float)prm1, rbf, (float)epsa,
+                                                             FLT_EPSILON * FLT_EPSILON, (float*)dF, lf, (float*)dD, lD);
+  }
+  count_launches(1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem kernel");
+  if (mem == BEM_MEM_HOST) {
+    cudaMemcpy2DAsync(F, esz * ldf, dF, esz * lf, esz * n, n, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpy2DAsync(D, esz * ldd, dD, esz * lD, esz * dof * n, dof * n, cudaMemcpyDeviceToHost, c->stream);
+  }
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem");
+  return BEM_OK;
+}

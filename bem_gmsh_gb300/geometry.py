@@ -195,12 +195,14 @@ def discretize_curves(cad: np.ndarray, p: int):
 
 
 def from_cad(name, cad, p, properties, bc_type, bc_value, internal=None, region=None,
-             keep_geo=True) -> BEMdata:
+             keep_geo=True, discretize=None) -> BEMdata:
     """Build a BEMdata from CAD nodes `cad` (ne, ngeo, 2) and per-element BC data
-    `bc_type` (ne, ndof), `bc_value` (ne, ndof) or per-node arrays (n, ndof)."""
+    `bc_type` (ne, ndof), `bc_value` (ne, ndof) or per-node arrays (n, ndof).
+    `discretize(cad, p)` makes the nodes, normals, Jacobians, lengths and
+    weights (default: `discretize_curves` on the host)."""
     cad = np.asarray(cad, dtype=np.float64)
     ne = cad.shape[0]
-    nodes, normal, J, L, wi = discretize_curves(cad, p)
+    nodes, normal, J, L, wi = (discretize or discretize_curves)(cad, p)
     n = ne * (p + 1)
     ndof = properties.ndof
     bt = np.asarray(bc_type).reshape(-1, ndof)

@@ -159,6 +159,45 @@ def extra_configs(ctx):
     t = time.perf_counter()
     res = [adjoint_laplace(d, q, npg=16, ctx=ctx, return_stats=True) for (d, _), q in zip(cases, qts)]
     dt = time.perf_counter() - t
+    # DIBEM pairwise F, D over the C2 points (device buffers, kernel time)
+    import torch
+    from bem_gmsh_gb300 import _lib as L
+    from bem_gmsh_gb300.geometry import star_domain
+    d2 = star_domain(2731, p=2, seed=0)
+    nt = d2.nt
+    pts = torch.as_tensor(np.asarray(d2.collocation, np.float64)).cuda()
+    px, py = pts[:, 0].contiguous(), pts[:, 1].contiguous()
+    hbm_gbs = peaks()[0]
+    dib = {}
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    for name, tdt, dtid in (("fp32", torch.float32, L.BEM_F32), ("fp64", torch.float64, L.BEM_F64)):
+        ldx = (nt + 3) // 4 * 4
+        Fb = torch.empty((nt, ldx), dtype=tdt, device="cuda")
+        Db = torch.empty((nt, ldx), dtype=tdt, device="cuda")
+
+        def run():
+            rc = ctx.L.bem_dibem_fd2d(ctx.h, nt, px.data_ptr(), py.data_ptr(), 0, 1.0, 0.0, 3, 1e-16, dtid,
+                                      L.BEM_MEM_DEVICE, Fb.data_ptr(), ldx, Db.data_ptr(), ldx)
+            ctx.check(rc, "dibem_fd")
+        for _ in range(3):
+            run()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        for e0, e1 in ev:
+            e0.record(stream)
+            run()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / len(ev)
+        nbytes = 2.0 * nt * nt * Fb.element_size()
+        dib[name] = {"ms": ms, "entries_per_s": 2.0 * nt * nt / (ms * 1e-3),
+                     "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / hbm_gbs}
+        del Fb, Db
+    ctx.set_stream(0)
+    out["dibem_fd_c2"] = {"N": nt, "rbf": "PHS3", **dib,
+                          "note": "F and D (2 N^2 entries) written to device buffers; CUDA events on the "
+                                  "launching stream around each call (one launch, plus its launch latency)"}
     out["adjoint_c5"] = {
         "domains": len(cases), "nodes": cases[0][0].n, "seconds": dt, "gradients_per_s": len(cases) / dt,
         "ms_per_gradient": 1e3 * dt / len(cases),

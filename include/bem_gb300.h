@@ -213,6 +213,36 @@ int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, int npg, do
                                    void* cuda_stream);
 
 /*
+ * Dense pairwise DIBEM matrices over the nt collocation points (x, y):
+ * F_ij = phi(R) and D_ij = fundamental solution, i != j, R = |x_j - x_i| --
+ * replaces `_dibem_FD_ka` / `_dibem_FD_kernel!` (src/Laplace/DIBEM_GPU.jl:179-208,
+ * kind 0 Laplace, prm0 = k, D nt x nt) and `_elast_dibem_FD_kernel!`
+ * (src/Elasticity/Assembly_GPU.jl:258-280, kind 1 Kelvin, prm0 = mu, prm1 =
+ * effective nu, D 2nt x 2nt of 2x2 U blocks).  rbf: 1-7 polyharmonic
+ * splines, 10 fundamental solution (`_gpu_rbf_kind`, DIBEM_GPU.jl:103-114);
+ * epsa: the log shift (`AVOID_INF` = 1e-16 in the reference).  dtype BEM_F32
+ * computes and stores FP32, BEM_F64 FP64.  F, D column-major.
+ */
+int bem_dibem_fd2d(bem_ctx* ctx, int nt, const double* px, const double* py, int kind, double prm0, double prm1,
+                   int rbf, double epsa, int dtype, int mem, void* F, int64_t ldf, void* D, int64_t ldd);
+
+/*
+ * Boundary discretisation: ne elements, each given by ngeo equispaced CAD
+ * nodes (cad_x/cad_y [ne*ngeo], element-major), to p+1 collocation nodes per
+ * element at the Gauss-Legendre points with the Jacobian |dx/dxi|, the
+ * outward normal (tangent rotated by -90 degrees) and the element length
+ * |sum_k J_k w_k| -- the geometry loop of `format2d`
+ * (src/Core/Input.jl:163-185) and `bemdata_from_loops`
+ * (src/Topology/Topology.jl:311-319).  Outputs px, py, nx, ny, jac [ne*(p+1)]
+ * and elen [ne] fill a bem_geom2d directly; elem_weight (host, [p+1]) gets
+ * the Gauss weights.  mem says where cad_* and the outputs live (elem_weight
+ * is always host).  2 <= ngeo <= 6, 0 <= p <= 5.
+ */
+int bem_discretize2d(bem_ctx* ctx, int ne, int ngeo, int p, const double* cad_x, const double* cad_y, int mem,
+                     double* px, double* py, double* nx, double* ny, double* jac, double* elen,
+                     double* elem_weight);
+
+/*
  * Shape gradient by the adjoint method (no reference counterpart; built on
  * the path's assembly and solve, src/Core/Assembly_full.jl:61-175 and
  * src/Core/Boundary_conditions.jl:20-75).  Laplace, elements with their

@@ -1384,6 +1384,55 @@ int orc_near_element(const double* xy, int nn, double L, double pfx, double pfy,
 // 152-174): A = H with BC==0 columns replaced by -G[:,j];
 // b = sum_{BC==0} -H[:,j] BV_j + sum_{BC!=0} G[:,j] BV_j.
 // rows x rows A, cols = number of boundary DOFs.
+// _dibem_FD_kernel! / _elast_dibem_FD_kernel! (src/Laplace/DIBEM_GPU.jl:194-208,
+// src/Elasticity/Assembly_GPU.jl:258-280) with _dibem_phi (DIBEM_GPU.jl:116-139)
+static double dibem_phi(int kind, double R, double k, double epsa) {
+  const double R2 = R * R;
+  switch (kind) {
+    case 1: return R;
+    case 2: return R2 * std::log(R + epsa);
+    case 3: return R2 * R;
+    case 4: return (R2 * R2) * std::log(R + epsa);
+    case 5: return R2 * R2 * R;
+    case 6: return (R2 * R2 * R2) * std::log(R + epsa);
+    case 7: return R2 * R2 * R2 * R;
+    default: return -std::log(R) / (2.0 * kPi * k);
+  }
+}
+
+void orc_dibem_fd2d(int nt, const double* px, const double* py, int kind, double prm0, double prm1, int rbf,
+                    double epsa, double* F, double* D) {
+  const int dof = kind == 0 ? 1 : 2;
+  const int64_t ldd = (int64_t)dof * nt;
+  for (int64_t q = 0; q < (int64_t)nt * nt; ++q) F[q] = 0.0;
+  for (int64_t q = 0; q < ldd * ldd; ++q) D[q] = 0.0;
+  const double eps2 = kEps * kEps;
+  for (int j = 0; j < nt; ++j)
+    for (int i = 0; i < nt; ++i) {
+      if (i == j) continue;
+      const double rx = px[j] - px[i], ry = py[j] - py[i];
+      const double R2 = rx * rx + ry * ry;
+      if (!(R2 > eps2)) continue;
+      const double R = std::sqrt(R2);
+      if (kind == 0) {
+        D[i + (int64_t)j * nt] = -std::log(R) * (1.0 / (2.0 * kPi)) / prm0;
+        F[i + (int64_t)j * nt] = dibem_phi(rbf, R, prm0, epsa);
+      } else {
+        F[i + (int64_t)j * nt] = dibem_phi(rbf, R, 1.0, epsa);
+        const double mu = prm0, nu = prm1;
+        const double dr1 = rx / R, dr2 = ry / R;
+        const double prod1 = 4.0 * kPi * (1.0 - nu);
+        const double prod2 = (3.0 - 4.0 * nu) * (-std::log(R));
+        const double base = 2.0 * prod1 * mu;
+        const double u11 = (prod2 + dr1 * dr1) / base, u12 = (dr1 * dr2) / base, u22 = (prod2 + dr2 * dr2) / base;
+        D[2 * i + (int64_t)(2 * j) * ldd] = u11;
+        D[2 * i + 1 + (int64_t)(2 * j) * ldd] = u12;
+        D[2 * i + (int64_t)(2 * j + 1) * ldd] = u12;
+        D[2 * i + 1 + (int64_t)(2 * j + 1) * ldd] = u22;
+      }
+    }
+}
+
 // interior_laplace (src/Laplace/Lubrication.jl:399-416): potential at m
 // interior points, every element through integrate_element.
 int orc_interior_laplace(const OrcGeom* og, double k, int npg, int nearfield, const double* T,

@@ -76,6 +76,7 @@ def lib():
         _lib.orc_strain_stress2d.argtypes = [ctypes.POINTER(OrcGeom), d, d, P, P, P, P]
         _lib.orc_interior_laplace.argtypes = [ctypes.POINTER(OrcGeom), d, i, i, P, P, i, P, P, P]
         _lib.orc_interior_laplace.restype = i
+        _lib.orc_dibem_fd2d.argtypes = [i, P, P, i, d, d, i, d, P, P]
     return _lib
 
 
@@ -185,6 +186,46 @@ def split_sol(dad, x):
     t = np.where(BC == 0, x[:nb], BV)
     dad.set_cache(u=u, traction=t, T=u, x=np.asarray(x))
     return u
+
+
+def dibem_fd(pts, kind=0, prm0=1.0, prm1=0.0, rbf=3, epsa=1e-16):
+    """Pairwise DIBEM F, D (`_dibem_FD_kernel!`, src/Laplace/DIBEM_GPU.jl:194-208;
+    Kelvin `_elast_dibem_FD_kernel!`, src/Elasticity/Assembly_GPU.jl:258-280)."""
+    pts = np.asarray(pts, np.float64).reshape(-1, 2)
+    nt = len(pts)
+    dof = 1 if kind == 0 else 2
+    px, py = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+    F = np.zeros((nt, nt), order="F")
+    D = np.zeros((dof * nt, dof * nt), order="F")
+    lib().orc_dibem_fd2d(nt, _p(px), _p(py), kind, float(prm0), float(prm1), int(rbf), float(epsa), _p(F), _p(D))
+    return F, D
+
+
+def discretize(cad, p):
+    """Collocation nodes, normals, Jacobians, element lengths and weights of
+    elements given by equispaced CAD nodes `cad` (ne, ngeo, 2): the geometry
+    loop of `format2d` (src/Core/Input.jl:163-185): nodes = Ngeo*X,
+    dx = dNgeo*X, J = |dx|, normal = tan2normal(dx/J) = (t_y, -t_x),
+    L = |J . w| with Gauss-Legendre (qsi, w) of p+1 points
+    (`discontinuous_nodes_weights`).  Basis from monomial coefficients, Gauss
+    points from numpy's leggauss."""
+    cad = np.asarray(cad, np.float64)
+    ngeo = cad.shape[1]
+    qsi, w = np.polynomial.legendre.leggauss(p + 1)
+    t = np.linspace(-1.0, 1.0, ngeo)
+    N = np.empty((p + 1, ngeo))
+    dN = np.empty((p + 1, ngeo))
+    for m in range(ngeo):
+        c = np.poly(np.delete(t, m))
+        c = c / np.polyval(c, t[m])
+        N[:, m] = np.polyval(c, qsi)
+        dN[:, m] = np.polyval(np.polyder(c), qsi)
+    nodes = np.einsum("qm,emd->eqd", N, cad)
+    dx = np.einsum("qm,emd->eqd", dN, cad)
+    J = np.hypot(dx[..., 0], dx[..., 1])
+    normal = np.stack([dx[..., 1] / J, -dx[..., 0] / J], axis=-1)
+    L = np.abs(J @ w)
+    return nodes, normal, J, L, w
 
 
 def interior_laplace(dad, pts, npg=16, nearfield="tanp3c", T=None, q=None):

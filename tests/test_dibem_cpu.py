@@ -1,0 +1,37 @@
+"""Pairwise DIBEM matrices in the oracle (`_dibem_FD_kernel!`,
+src/Laplace/DIBEM_GPU.jl:194-208; `_elast_dibem_FD_kernel!`,
+src/Elasticity/Assembly_GPU.jl:258-280): closed-form entries and symmetry."""
+import math
+
+import numpy as np
+import pytest
+
+
+@pytest.mark.parametrize("rbf,phi", [
+    (1, lambda R: R), (2, lambda R: R * R * math.log(R + 1e-16)), (3, lambda R: R ** 3),
+    (4, lambda R: R ** 4 * math.log(R + 1e-16)), (5, lambda R: R ** 5),
+    (6, lambda R: R ** 6 * math.log(R + 1e-16)), (7, lambda R: R ** 7),
+    (10, lambda R: -math.log(R) / (2 * math.pi * 2.0)),
+])
+def test_laplace_entries(orc, rbf, phi):
+    pts = np.array([[0.0, 0.0], [2.0, 0.0], [0.5, 1.5]])
+    F, D = orc.dibem_fd(pts, kind=0, prm0=2.0, rbf=rbf)
+    R = 2.0
+    assert F[0, 1] == pytest.approx(phi(R), rel=1e-15)
+    assert D[0, 1] == pytest.approx(-math.log(R) / (2 * math.pi) / 2.0, rel=1e-15)
+    assert np.all(np.diag(F) == 0) and np.all(np.diag(D) == 0)
+    np.testing.assert_allclose(F, F.T, rtol=1e-15)
+    np.testing.assert_allclose(D, D.T, rtol=1e-15)
+
+
+def test_kelvin_blocks(orc):
+    mu, nu = 80.0, 0.3
+    pts = np.array([[0.0, 0.0], [0.6, 0.8], [-1.0, 0.5], [0.2, -0.7]])
+    F, D = orc.dibem_fd(pts, kind=1, prm0=mu, prm1=nu, rbf=3)
+    assert D.shape == (8, 8) and F.shape == (4, 4)
+    # block (0, 1): r = (0.6, 0.8), R = 1
+    base = 2 * 4 * math.pi * (1 - nu) * mu
+    assert D[0, 2] == pytest.approx(0.36 / base, rel=1e-14)
+    assert D[0, 3] == pytest.approx(0.48 / base, rel=1e-14)
+    assert D[1, 3] == pytest.approx(0.64 / base, rel=1e-14)
+    np.testing.assert_allclose(D, D.T, rtol=1e-14, atol=0)
