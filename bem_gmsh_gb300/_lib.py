@@ -151,6 +151,13 @@ class Context:
     def launch_count(self) -> int:
         return int(self.L.bem_launch_count())
 
+    def selftest_gemm(self, n: int):
+        """Bulk trailing update of one LU step on an n x n matrix, timed alone:
+        (ms per launch, algorithmic GB/s, TF32 TFLOP/s)."""
+        out = (ctypes.c_double * 4)()
+        self.check(self.L.bem_selftest(self.h, 3, n, out), "selftest")
+        return out[0], out[1], out[2]
+
     def selftest_diag(self, n: int = 128):
         """Blocked vs Gauss-Jordan factorization of one 128 x 128 block:
         (max |diff L\\U|, max |L\\U|, max |diff inverses|, max |inverse|)."""

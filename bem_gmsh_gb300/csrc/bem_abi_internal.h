@@ -17,7 +17,7 @@ struct bem_ctx {
     SLOT_PAIRS, SLOT_BC, SLOT_BV, SLOT_OUT0, SLOT_OUT1, SLOT_OUT2, SLOT_OUT3,
     SLOT_LU0, SLOT_LU1, SLOT_LU2, SLOT_LU3, SLOT_LU4, SLOT_LU5, SLOT_LU6, SLOT_LU7,
     SLOT_TC0, SLOT_TC1, SLOT_TC2, SLOT_TC3, SLOT_TC4, SLOT_TC5, SLOT_TEST0, SLOT_TEST1,
-    SLOT_NODES_DF, SLOT_LOGTAB, SLOT_ADJ0, SLOT_ADJ1,
+    SLOT_NODES_DF, SLOT_LOGTAB, SLOT_ADJ0, SLOT_ADJ1, SLOT_LU8,
     NSLOT
   };
   struct Buf {

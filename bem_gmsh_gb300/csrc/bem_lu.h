@@ -22,7 +22,10 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
 // forward result); tags: 2 Npad words of (epoch, value) scratch, zeroed
 // before the first call; epoch: > 0 and different in every call on the same
 // tags; err: timeout flag.  r may be clobbered.  Returns 0 or a CUDA error.
-int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
+// M_b couplings of the triangular sweeps (Mc: K * 2 * 128^2 floats), after
+// the factorization
+void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float* Mc, cudaStream_t st);
+int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st);
 
 void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,

@@ -449,10 +449,57 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// M^L_b = Linv_b L_{b,b-1} (b >= 1) and M^U_b = Uinv_b U_{b,b+1} (b <= K-2),
+// column-major in Mc[(2 b + side) 128^2]: the coupling of block b of a
+// triangular sweep to the block solved just before it.  With
+//   z_b = D_b (r_b - sum over the other solved blocks),  y_b = z_b - M_b y_prev
+// the sweep's dependent step is one 128 x 128 product; z_b is formed while
+// the previous block is still being solved.  One CTA per (block, side),
+// 8 x 8 outputs per thread.
+constexpr int CPL_LD = LU_NB + 1;
+constexpr int CPL_SMEM = (int)sizeof(float) * 2 * LU_NB * CPL_LD;
+
+__global__ void __launch_bounds__(256) k_lu_couplings(const float* __restrict__ A, int64_t ld, int K,
+                                                      const float* __restrict__ Dinv, float* __restrict__ Mc) {
+  extern __shared__ float cs_[];
+  const int b = blockIdx.x, side = blockIdx.y, t = threadIdx.x;
+  if (side == 0 ? b == 0 : b == K - 1) return;
+  float* P = cs_;                  // D_b, [col][row]
+  float* Q = cs_ + LU_NB * CPL_LD;  // coupling block of A, [col][row]
+  const float* Pg = Dinv + (size_t)b * 2 * LU_NB * LU_NB + (side ? LU_NB * LU_NB : 0);
+  const int qb = side ? b + 1 : b - 1;
+  const float* Qg = A + (size_t)b * LU_NB + (size_t)qb * LU_NB * ld;
+  for (int idx = t; idx < LU_NB * LU_NB; idx += 256) {
+    const int r = idx & (LU_NB - 1), c = idx >> 7;
+    P[c * CPL_LD + r] = Pg[r + (size_t)c * LU_NB];
+    Q[c * CPL_LD + r] = Qg[r + (size_t)c * ld];
+  }
+  __syncthreads();
+  const int r0 = (t >> 4) * 8, c0 = (t & 15) * 8;
+  float acc[8][8] = {};
+  for (int k = 0; k < LU_NB; ++k) {
+    float a[8], q[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = P[k * CPL_LD + r0 + i];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) q[j] = Q[(c0 + j) * CPL_LD + k];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], q[j], acc[i][j]);
+  }
+  float* Mo = Mc + (size_t)(2 * b + side) * LU_NB * LU_NB;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) Mo[(size_t)(c0 + j) * LU_NB + r0 + i] = acc[i][j];
+}
+
 template <bool UPPER>
 __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, int64_t ld, int K,
-                                                   const float* __restrict__ Dinv, const float* r,
-                                                   float* y, unsigned long long* tags, int epoch, int* err) {
+                                                   const float* __restrict__ Dinv, const float* __restrict__ Mc,
+                                                   const float* r, float* y, unsigned long long* tags, int epoch,
+                                                   int* err) {
   extern __shared__ float Ds[];  // the block's inverse, [col][row], LU_NB * (LU_NB + 1)
   __shared__ float ys[LU_NB];
   __shared__ float part[2][LU_NB];
@@ -468,15 +515,17 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
   if (t == 0) bad = 0;
   float acc = (half == 0) ? r[rb + row] : 0.f;
   const int nj = UPPER ? (K - 1 - b) : b;
-  __syncthreads();
-  for (int s = 0; s < nj; ++s) {
-    const int j = UPPER ? (K - 1 - s) : s;
-    // prefetch this thread's 64 coefficients of block (b, j) before waiting
-    float pre[LU_NB / 2];
-    const float* P = A + (rb + row) + ((size_t)j * LU_NB + half * (LU_NB / 2)) * ld;
+  // this thread's half row of the coupling to the adjacent block
+  float mreg[LU_NB / 2];
+  if (nj > 0) {
+    const float* Mb = Mc + (size_t)(2 * b + (UPPER ? 1 : 0)) * LU_NB * LU_NB;
 #pragma unroll
-    for (int q = 0; q < LU_NB / 2; ++q) pre[q] = P[(size_t)q * ld];
-    // y_j arrives as (epoch, value) words: each thread waits for its own
+    for (int q = 0; q < LU_NB / 2; ++q) mreg[q] = Mb[(size_t)(half * (LU_NB / 2) + q) * LU_NB + row];
+  }
+  __syncthreads();
+  // waits for y_j: each of the first 128 threads polls its own (epoch, value)
+  // word; false when the wait ran out
+  auto fetch = [&](int j) {
     if (t < LU_NB) {
       const unsigned long long* w = tags + (size_t)j * LU_NB + t;
       unsigned long long v = ld_acquire_u64(w);
@@ -492,7 +541,17 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
       ys[t] = __uint_as_float((uint32_t)v);
     }
     __syncthreads();
-    if (bad) {
+    return bad == 0;
+  };
+  // every solved block but the adjacent one
+  for (int s = 0; s + 1 < nj; ++s) {
+    const int j = UPPER ? (K - 1 - s) : s;
+    // prefetch this thread's 64 coefficients of block (b, j) before waiting
+    float pre[LU_NB / 2];
+    const float* P = A + (rb + row) + ((size_t)j * LU_NB + half * (LU_NB / 2)) * ld;
+#pragma unroll
+    for (int q = 0; q < LU_NB / 2; ++q) pre[q] = P[(size_t)q * ld];
+    if (!fetch(j)) {
       if (t == 0) atomicExch(err, 1);
       return;
     }
@@ -500,20 +559,40 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     for (int q = 0; q < LU_NB / 2; ++q) acc -= pre[q] * ys[half * (LU_NB / 2) + q];
     __syncthreads();
   }
+  // z_b = D_b (r_b - ...)
   part[half][row] = acc;
   __syncthreads();
   if (t < LU_NB) ys[t] = part[0][t] + part[1][t];
   __syncthreads();
-  // y_b = D_b * (r_b - ...)
-  float o = 0.f;
+  float o0 = 0.f, o1 = 0.f;
 #pragma unroll 16
-  for (int q = half * (LU_NB / 2); q < (half + 1) * (LU_NB / 2); ++q) o += Ds[q * (LU_NB + 1) + row] * ys[q];
-  part[half][row] = o;
+  for (int q = half * (LU_NB / 2); q < (half + 1) * (LU_NB / 2); q += 2) {
+    o0 += Ds[q * (LU_NB + 1) + row] * ys[q];
+    o1 += Ds[(q + 1) * (LU_NB + 1) + row] * ys[q + 1];
+  }
+  part[half][row] = o0 + o1;
   __syncthreads();
+  float yb = (t < LU_NB) ? part[0][t] + part[1][t] : 0.f;
+  if (nj > 0) {
+    // y_b = z_b - M_b y_adjacent
+    __syncthreads();  // part and ys are reused
+    if (!fetch(UPPER ? b + 1 : b - 1)) {
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
+    float m0 = 0.f, m1 = 0.f;
+#pragma unroll
+    for (int q = 0; q < LU_NB / 2; q += 2) {
+      m0 = fmaf(mreg[q], ys[half * (LU_NB / 2) + q], m0);
+      m1 = fmaf(mreg[q + 1], ys[half * (LU_NB / 2) + q + 1], m1);
+    }
+    part[half][row] = m0 + m1;
+    __syncthreads();
+    if (t < LU_NB) yb -= part[0][t] + part[1][t];
+  }
   if (t < LU_NB) {
-    const float v = part[0][t] + part[1][t];
-    y[rb + t] = v;
-    st_relaxed_u64(tags + rb + t, ((unsigned long long)(unsigned)epoch << 32) | __float_as_uint(v));
+    y[rb + t] = yb;
+    st_relaxed_u64(tags + rb + t, ((unsigned long long)(unsigned)epoch << 32) | __float_as_uint(yb));
   }
 }
 
@@ -1224,7 +1303,19 @@ static void lu_solve_vec_steps(const float* A, int64_t ld, int Npad, const float
 
 // y = (L U)^{-1} r on a padded FP32 vector.  r is overwritten with the
 // forward result; the solution lands in `out`.  flags: 2K ints of scratch.
-int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float* r, float* tmp,
+void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float* Mc, cudaStream_t st) {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_lu_couplings, cudaFuncAttributeMaxDynamicSharedMemorySize, CPL_SMEM);
+  });
+  const int K = Npad / LU_NB;
+  if (K < 2) return;
+  KScope ks(st, KC_TRSV);
+  count_launches(1);
+  k_lu_couplings<<<dim3(K, 2), 256, CPL_SMEM, st>>>(A, ld, K, Dinv, Mc);
+}
+
+int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st) {
   const int K = Npad / LU_NB;
   static int max_coresident = 0;
@@ -1250,7 +1341,7 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
   unsigned long long* t0 = tags;
   unsigned long long* t1 = tags + Npad;
   {
-    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&r, (void*)&tmp,
+    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&r, (void*)&tmp,
                     (void*)&t0, (void*)&epoch, (void*)&err};
     // forward: r -> tmp (separate output so that no CTA reads a block another rewrote)
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, dim3(K), dim3(256), args,
@@ -1258,7 +1349,7 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, float*
     if (e != cudaSuccess) return (int)e;
   }
   {
-    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&tmp, (void*)&out,
+    void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&tmp, (void*)&out,
                     (void*)&t1, (void*)&epoch, (void*)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, dim3(K), dim3(256), args,
                                                 dsm, st);

@@ -118,7 +118,8 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   float* rf = (float*)c->get(bem_ctx::SLOT_LU6, sizeof(float) * (3 * (size_t)Npad + 64) +
                                                    sizeof(unsigned long long) * (2 * (size_t)Npad));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
-  if (!A32 || !cs || !Dinv || !V || !Z || !w || !rf || !info) return BEM_ERR_NOMEM;
+  float* Mc = (float*)c->get(bem_ctx::SLOT_LU8, sizeof(float) * (size_t)K * 2 * LU_NB * LU_NB);
+  if (!A32 || !cs || !Dinv || !V || !Z || !w || !rf || !info || !Mc) return BEM_ERR_NOMEM;
   double* hbuf = w + N;  // 64 doubles of scratch
   float* tmpf = rf + Npad;
   float* outf = rf + 2 * (size_t)Npad;
@@ -150,6 +151,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   else
     rc = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
   if (rc) return c->cuda_fail((cudaError_t)rc, "lu_factor");
+  bem::lu_couplings(A32, Npad, Npad, Dinv, Mc, st);
   tf.stop(st);
   int hinfo2[2] = {0, 0};
   cudaMemcpyAsync(hinfo2, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -169,7 +171,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   int prc = 0;
   auto precond = [&](const double* v, double* z) {
     bem::to_f32(v, N, Npad, rf, st);
-    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, rf, tmpf, outf, tags, ++epoch, werr, st);
+    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, Mc, rf, tmpf, outf, tags, ++epoch, werr, st);
     if (e2) prc = e2;
     bem::from_f32_scale(outf, cs, N, z, st);
   };
@@ -469,10 +471,49 @@ __global__ void k_maxdiff(const float* A, const float* B, int64_t cnt, float* ou
 // with the legacy mma.sync ones; out[0] = max |difference of the factors|,
 // out[1] = max |factor|, out[2] / out[3] = factor times (ms) tcgen05 / legacy.
 extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
-  if (!c || !out || (which != 1 && which != 2) || n < LU_NB || n % LU_NB != 0 || n > 16384)
+  if (!c || !out || which < 1 || which > 3 || n < LU_NB || n % LU_NB != 0 || n > 16384)
     return BEM_ERR_INVALID;
+  if (which == 3 && n < 2 * LU_NB) return BEM_ERR_INVALID;
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
+  if (which == 3) {
+    // the bulk trailing update of LU step 0 alone: C (n-128)^2 -= L21 U12,
+    // repeated; nothing else runs on the device meanwhile
+    float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
+    float* Lt = (float*)c->get(bem_ctx::SLOT_TC0, sizeof(float) * (size_t)n * LU_NB);
+    float* Ltlo = (float*)c->get(bem_ctx::SLOT_TC1, sizeof(float) * (size_t)n * LU_NB);
+    float* Ulo = (float*)c->get(bem_ctx::SLOT_TC2, sizeof(float) * (size_t)n * LU_NB);
+    int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
+    if (!A1 || !Lt || !Ltlo || !Ulo || !info) return BEM_ERR_NOMEM;
+    bem::TcPlan tcp;
+    if (!bem::tc_plan(tcp, A1, n, n, Lt, Ltlo, Ulo)) {
+      c->last_error = "tensor map encoding failed";
+      return BEM_ERR_UNSUPPORTED;
+    }
+    k_fill_test<<<1024, 256, 0, st>>>(A1, n, n, 4242u);
+    cudaMemsetAsync(info, 0, 16, st);
+    bem::tc_split(tcp, 0, st);
+    const int rem = n - LU_NB, reps = 20;
+    for (int i = 0; i < 3; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st);
+    Timer t;
+    t.start(st);
+    for (int i = 0; i < reps; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st);
+    t.stop(st);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, info + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "selftest gemm");
+    if (herr) {
+      c->last_error = "bulk update reported a barrier timeout";
+      return BEM_ERR_CUDA;
+    }
+    const double ms = t.ms() / reps;
+    out[0] = ms;
+    out[1] = 8.0 * (double)rem * rem / (ms * 1e-3) / 1e9;
+    out[2] = 3.0 * 2.0 * (double)rem * rem * LU_NB / (ms * 1e-3) / 1e12;
+    out[3] = 0.0;
+    return BEM_OK;
+  }
   if (which == 2) {
     float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
     float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);

@@ -305,7 +305,11 @@ int bem_strain_stress2d(bem_ctx* ctx, const bem_geom2d* geom, double lam, double
  * counterpart).  which = 1: factor an n x n test matrix (n a multiple of 128)
  * once with the tcgen05 trailing updates and once with the legacy mma.sync
  * updates; out[0] = max |difference of the factors|, out[1] = max |factor|,
- * out[2], out[3] = factorization times in ms (tcgen05, legacy).
+ * out[2], out[3] = factorization times in ms (tcgen05, legacy).  which = 2:
+ * the 128 x 128 diagonal-block factorization against a reference kernel.
+ * which = 3: the bulk trailing update of one LU step, C ((n-128)^2) -= L U,
+ * timed alone: out[0] ms per launch, out[1] algorithmic GB/s (C read and
+ * write), out[2] TF32 tensor TFLOP/s (three products).  n >= 256.
  */
 int bem_selftest(bem_ctx* ctx, int which, int n, double* out);
 
