@@ -17,7 +17,8 @@ BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
 BEM_OPT_TCGEN05 = 1
 BEM_OPT_KERNEL_TIMING = 2
 BEM_OPT_FAR_DF = 3
-KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total"]
+KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
+                  "lu_panels", "lu_thin"]
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "refinement did not converge", 5: "device wait timed out", 6: "unsupported"}

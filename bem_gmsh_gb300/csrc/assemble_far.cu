@@ -9,8 +9,11 @@
 //                   walks the tile's columns, so every warp store is one
 //                   coalesced 512-byte column segment.  Far pairs get nodal
 //                   lumping (`_far_nodal_scalar!`/`_far_nodal_vec!`,
-//                   Assembly_full.jl:801-822); a conservative FP32 bounding-box
-//                   test sends every pair that may be near to a pair list.
+//                   Assembly_full.jl:801-822); pairs that a conservative FP32
+//                   bounding-box test calls possibly near are skipped.
+//   near_classify_kernel  the same box test over all (point, element) pairs,
+//                   ahead of the far kernel, lists the possibly-near pairs, so
+//                   that the near kernel runs beside the far kernel.
 //   near_kernel     one thread per listed pair: the exact FP64 near test
 //                   (`_near_element`, :736-754), then the tanp3c near-singular
 //                   integral, or FP64 far lumping if the pair is far after all.
@@ -139,6 +142,47 @@ __global__ void pack_elems_kernel(GeomDev g, double near_factor, const unsigned 
   r.lim2 = (near_factor > 1e20) ? INFINITY : __double2float_ru(limw * limw);
   r.pad0 = r.pad1 = r.pad2 = 0.f;
   el[e] = r;
+}
+
+// Conservative box test of a source point (x, y) against an element record:
+// true when the pair is far for the exact FP64 test as well.  Explicit
+// round-to-nearest operations, so that the classification kernel and the far
+// kernel agree bit for bit.
+__device__ __forceinline__ bool box_far(float xh, float xl, float yh, float yl, const ElemRec& E) {
+  const float x = __fadd_rn(xh, xl), y = __fadd_rn(yh, yl);
+  const float dx = fmaxf(fmaxf(__fsub_rn(E.lox, x), __fsub_rn(x, E.hix)), 0.f);
+  const float dy = fmaxf(fmaxf(__fsub_rn(E.loy, y), __fsub_rn(y, E.hiy)), 0.f);
+  return __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) > E.lim2;
+}
+
+// Possibly-near (point, element) pairs into the pair list: one thread per
+// point, the CTA's 256 elements staged in shared memory.
+__global__ void __launch_bounds__(256) near_classify_kernel(int nt, int ne, const float4* __restrict__ rows,
+                                                            const ElemRec* __restrict__ elems,
+                                                            int* pair_count, int2* pairs, int pair_cap) {
+  __shared__ ElemRec s_e[256];
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  const int e0 = blockIdx.y * 256;
+  const int nel = min(256, ne - e0);
+  if ((int)threadIdx.x < nel) s_e[threadIdx.x] = elems[e0 + threadIdx.x];
+  __syncthreads();
+  const bool valid = i < nt;
+  const float4 r = rows[valid ? i : nt - 1];
+  const int lane = threadIdx.x & 31;
+  for (int el = 0; el < nel; ++el) {
+    const bool need = valid && !box_far(r.x, r.y, r.z, r.w, s_e[el]);
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(pair_count, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const int slot = base + __popc(m & ((1u << lane) - 1));
+        if (slot < pair_cap) pairs[slot] = make_int2(i, e0 + el);
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -329,27 +373,11 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
   for (int el = lane_e; el < ne_t; el += EL) {
     const ElemRec E = s_el[el];
     const int e = e0 + el;
-    // conservative box test per source point
+    // conservative box test per source point (the possibly-near pairs are
+    // listed by near_classify_kernel with the same test)
     bool far[SPT];
 #pragma unroll
-    for (int s = 0; s < SPT; ++s) {
-      float x = sxh[s] + sxl[s], y = syh[s] + syl[s];
-      float dx = fmaxf(fmaxf(E.lox - x, x - E.hix), 0.f);
-      float dy = fmaxf(fmaxf(E.loy - y, y - E.hiy), 0.f);
-      far[s] = (dx * dx + dy * dy > E.lim2) || !valid[s];
-      bool need = valid[s] && !far[s];
-      unsigned m = __ballot_sync(0xffffffffu, need);
-      if (m) {
-        int leader = __ffs(m) - 1;
-        int base = 0;
-        if (rg == leader) base = atomicAdd(a.pair_count, __popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (need) {
-          int slot = base + __popc(m & ((1u << rg) - 1));
-          if (slot < a.pair_cap) a.pairs[slot] = make_int2(src0 + s, e);
-        }
-      }
-    }
+    for (int s = 0; s < SPT; ++s) far[s] = box_far(sxh[s], sxl[s], syh[s], syl[s], E) || !valid[s];
     if constexpr (PREC == 3) {
       static_assert(NC == 1 && FUSED, "double-float far field: fused Laplace only");
       const df::LogEntry* tab = (const df::LogEntry*)s_log;
@@ -574,12 +602,27 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   // the on-element rows need neither the far results nor the pair list: on
   // a side stream they run beside the far and near kernels (every kernel
   // writes its own entries; row sums are atomic)
+  {
+    KScope ks(st, KC_NEAR);
+    dim3 cg((g.nt + 255) / 256, (g.ne + 255) / 256);
+    near_classify_kernel<<<cg, 256, 0, st>>>(g.nt, g.ne, q.rows, q.elems, q.counters, q.pairs, q.pair_cap);
+  }
   const bool side = q.aux != nullptr && g.n > 0;
+  const bool side2 = side && q.aux2 != nullptr;
   if (side) {
     cudaEventRecord(q.ev_fork, st);
     cudaStreamWaitEvent(q.aux, q.ev_fork, 0);
     launch_singular(na, NC, g.n, q.aux);
     cudaEventRecord(q.ev_join, q.aux);
+  }
+  if (side2) {
+    // the near pairs (FP64 pipe) beside the far kernel (FP32 pipe)
+    cudaStreamWaitEvent(q.aux2, q.ev_fork, 0);
+    {
+      KScope ks(q.aux2, KC_NEAR);
+      launch_near_pairs(na, NC, q.aux2);
+    }
+    cudaEventRecord(q.ev_join2, q.aux2);
   }
   constexpr int SPT = RPT / DOF;
   dim3 grid((g.nt + 32 * SPT - 1) / (32 * SPT), (g.ne + 31) / 32);
@@ -589,12 +632,13 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   }
   {
     KScope ks(st, KC_NEAR);
-    launch_near_pairs(na, NC, st);
+    if (!side2) launch_near_pairs(na, NC, st);
     if (!side) launch_singular(na, NC, g.n, st);
     if (side) cudaStreamWaitEvent(st, q.ev_join, 0);
+    if (side2) cudaStreamWaitEvent(st, q.ev_join2, 0);
     launch_finalize(fi, NC, g.nt, st);
   }
-  count_launches(g.n > 0 ? 8 : 7);
+  count_launches(g.n > 0 ? 9 : 8);
 }
 
 int launch_assembly(const AsmRequest& q, cudaStream_t st) {

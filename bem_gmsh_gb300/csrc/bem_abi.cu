@@ -196,7 +196,9 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   for (auto e : c->events) cudaEventDestroy(e);
   if (c->asm_fork) cudaEventDestroy(c->asm_fork);
   if (c->asm_join) cudaEventDestroy(c->asm_join);
+  if (c->asm_join2) cudaEventDestroy(c->asm_join2);
   if (c->asm_stream) cudaStreamDestroy(c->asm_stream);
+  if (c->asm_stream2) cudaStreamDestroy(c->asm_stream2);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -302,13 +304,17 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     if (cudaStreamCreateWithPriority(&c->asm_stream, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&c->asm_stream2, cudaStreamNonBlocking, hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->asm_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->asm_join, cudaEventDisableTiming) != cudaSuccess)
-      return c->cuda_fail(cudaGetLastError(), "assembly side stream");
+        cudaEventCreateWithFlags(&c->asm_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->asm_join2, cudaEventDisableTiming) != cudaSuccess)
+      return c->cuda_fail(cudaGetLastError(), "assembly side streams");
   }
   q.aux = c->asm_stream;
+  q.aux2 = c->asm_stream2;
   q.ev_fork = c->asm_fork;
   q.ev_join = c->asm_join;
+  q.ev_join2 = c->asm_join2;
   if (q.prec == 3) {
     q.nodes_df = (bem::NodeDF*)c->get(bem_ctx::SLOT_NODES_DF, sizeof(bem::NodeDF) * (size_t)q.g.n);
     q.logtab = (float4*)c->get(bem_ctx::SLOT_LOGTAB, sizeof(float4) * 136);

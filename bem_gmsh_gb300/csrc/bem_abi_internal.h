@@ -35,8 +35,8 @@ struct bem_ctx {
   void* cusolver_handle = nullptr;  // FP64 comparison path (created on first use)
   std::vector<bem_ctx*> workers;    // sub-contexts of batched calls (own streams)
   // side stream and events of the assembly (created on first use)
-  cudaStream_t asm_stream = nullptr;
-  cudaEvent_t asm_fork = nullptr, asm_join = nullptr;
+  cudaStream_t asm_stream = nullptr, asm_stream2 = nullptr;
+  cudaEvent_t asm_fork = nullptr, asm_join = nullptr, asm_join2 = nullptr;
   bem::KProf prof;      // BEM_OPT_KERNEL_TIMING
 
   // second stream and events of the lookahead LU (created on first use)

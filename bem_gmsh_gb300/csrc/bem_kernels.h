@@ -123,8 +123,8 @@ struct AsmRequest {
   unsigned long long* absmax;  // scratch: largest |coordinate|
   // optional side stream for the on-element kernel (runs beside the far and
   // near kernels; joined before the diagonal), with its fork/join events
-  cudaStream_t aux = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t aux = nullptr, aux2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
 };
 
 // Launch the whole assembly on `stream` (asynchronous).  Returns 0 or a

@@ -18,7 +18,10 @@ enum KClass {
   KC_TRSV = 5,       // triangular solves
   KC_GEMV = 6,       // FP64 matrix-vector products / residuals
   KC_LU_TOTAL = 7,   // whole factorization
-  KC_COUNT = 8
+  KC_LU_DIAG = 8,    // diagonal-block factorizations (within KC_LU_CRIT)
+  KC_LU_PANELS = 9,  // block row / column panels (within KC_LU_CRIT)
+  KC_LU_THIN = 10,   // look-ahead updates of the next block row / column (within KC_LU_CRIT)
+  KC_COUNT = 11
 };
 
 struct KProf {

@@ -81,6 +81,35 @@ DF_HD double dfrom(uint64_t u) {
 #endif
 }
 
+DF_HD uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  std::memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+
+// (float)(v * 2^s) on the integer pipes: the exponent field gets s added and
+// the 52-bit fraction is rounded to 23 bits to nearest, ties to even.  Zeros
+// give signed zeros; a result outside the normal FP32 range, or an infinite
+// or NaN v, takes the FP64 multiply and conversion.
+DF_HD float scale_to_f32(double v, int s) {
+  const uint64_t b = dbits(v);
+  const uint32_t sign = (uint32_t)(b >> 63) << 31;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  if (ex == 0 && m == 0) return ffrom(sign);
+  const int E = ex + s - 1023 + 127;
+  if (ex == 0x7FF || E < 1 || E > 254) return (float)(v * dfrom((uint64_t)(1023 + s) << 52));
+  const uint32_t top = (uint32_t)(m >> 29);
+  const uint32_t rest = (uint32_t)(m & 0x1FFFFFFFu);
+  uint32_t out = sign | ((uint32_t)E << 23) | top;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (top & 1u))) out += 1u;
+  return ffrom(out);
+}
+
 // exact float of a small integer (|i| < 2^22) with one FP32 add (keeps the
 // int-to-float conversion off the FP64/conversion pipe)
 DF_HD float small_int_to_float(int i) { return sub_(ffrom(0x4B400000u + (uint32_t)i), 12582912.0f); }

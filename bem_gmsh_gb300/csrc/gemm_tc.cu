@@ -14,11 +14,11 @@
 //                      (column ranges); C read/modify/write coalesced per
 //                      column (a warp covers 32 consecutive rows), its first
 //                      columns loaded before the roles start.
-// The default (one 96 KB stage, 4 warps, 120 registers) keeps two CTAs on
-// each SM (2 x 256 TMEM columns), so that one tile's epilogue traffic
-// overlaps the other's loads and MMAs; measured alone on a 8064^2 update it
-// beats the 2-stage / 8-warp single-CTA form by 10 % and the whole solve by
-// 3 %.
+// The default (16-wide k chunks with the 64-byte swizzle, two 48 KB stages,
+// 4 warps, 120 registers) keeps two CTAs on each SM (2 x 256 TMEM columns),
+// so that one tile's epilogue traffic overlaps the other's loads and MMAs;
+// measured alone on a 8064^2 update it beats the 32-wide 2-stage / 8-warp
+// single-CTA form by 12 % and the whole solve by 4 %.
 // The tensor core reads the top 19 bits of an FP32 operand (TF32), so the
 // FP32 matrix itself is the "hi" operand; the "lo" operands x - tf32(x) are
 // precomputed by k_split_lo.  Every mbarrier wait is bounded: on timeout
@@ -38,17 +38,25 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int BN = 256;
-constexpr int BK = 32;  // one 128-byte swizzle atom of FP32
-#define BEM_TC_STAGES 1
+#define BEM_TC_BK 16
+// k chunk: one swizzle atom of FP32, 128-byte swizzle for 32, 64-byte for 16
+constexpr int BK = BEM_TC_BK;
+static_assert(BK == 32 || BK == 16, "BK must be 16 or 32");
+constexpr int SW_BYTES = BK * 4;           // swizzle span (bytes per row)
+constexpr int SW_SBO = 8 * SW_BYTES;       // 8-row group stride in shared memory
+constexpr uint64_t SW_LAYOUT = BK == 32 ? 2 : 4;  // descriptor layout: 128B / 64B swizzle
+#define BEM_TC_STAGES 2
 #define BEM_TC_WARPS 4
 constexpr int STAGES = BEM_TC_STAGES;
 constexpr int WARPS = BEM_TC_WARPS;  // epilogue warps: 4 (all columns each) or 8 (column halves)
 constexpr int THREADS = 32 * WARPS;
-constexpr int MIN_BLOCKS = (STAGES == 1 && WARPS <= 8) ? 2 : 1;
-constexpr int A_BYTES = BM * BK * 4;  // 16 KB
-constexpr int B_BYTES = BN * BK * 4;  // 32 KB
+constexpr int A_BYTES = BM * BK * 4;  // 16 KB at BK = 32
+constexpr int B_BYTES = BN * BK * 4;  // 32 KB at BK = 32
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+static_assert(8 * (2 * STAGES + 1) + 16 <= 256, "barrier area");
+// two CTAs per SM when their shared memory fits (registers capped at 128)
+constexpr int MIN_BLOCKS = (SMEM_BYTES <= 110 * 1024 && WARPS <= 8) ? 2 : 1;
 constexpr uint32_t TMEM_COLS = 256;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -85,15 +93,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (SBO), leading offset unused for this layout (1).
+// shared-memory matrix descriptor: K-major, swizzled rows of SW_BYTES, 8-row
+// groups SW_SBO bytes apart (SBO), leading offset unused for this layout (1).
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFF) >> 4);
   d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)(SW_SBO >> 4) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  d |= (uint64_t)2 << 61;  // SWIZZLE_128B
+  d |= SW_LAYOUT << 61;
   return d;
 }
 
@@ -149,20 +157,20 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_gemm_tc(const __grid_co
   const uint32_t base_u = smem_u32(dsm);
   const uint32_t tiles = (base_u + 1023u) & ~1023u;
   uint8_t* misc = dsm + (tiles - base_u) + STAGES * STAGE_BYTES;
-  uint64_t* bars = (uint64_t*)misc;  // full[2], empty[2], done
-  uint32_t* s_tmem = (uint32_t*)(misc + 64);
-  int* s_fail = (int*)(misc + 72);
+  uint64_t* bars = (uint64_t*)misc;  // full[STAGES], empty[STAGES], done
+  uint32_t* s_tmem = (uint32_t*)(misc + 8 * (2 * STAGES + 1));
+  int* s_fail = (int*)(misc + 8 * (2 * STAGES + 1) + 8);
   const uint32_t full0 = smem_u32(&bars[0]);
-  const uint32_t empty0 = smem_u32(&bars[2]);
-  const uint32_t done = smem_u32(&bars[4]);
+  const uint32_t empty0 = smem_u32(&bars[STAGES]);
+  const uint32_t done = smem_u32(&bars[2 * STAGES]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
 
   if (threadIdx.x == 0) {
-    mbar_init(full0, 1);
-    mbar_init(full0 + 8, 1);
-    mbar_init(empty0, 1);
-    mbar_init(empty0 + 8, 1);
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(full0 + 8 * i, 1);
+      mbar_init(empty0 + 8 * i, 1);
+    }
     mbar_init(done, 1);
     *s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_gemm_tc(const __grid_co
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *s_tmem;
-  constexpr int NCH = LU_NB / BK;  // 4 k chunks
+  constexpr int NCH = LU_NB / BK;  // k chunks
 
   // epilogue geometry: warp w owns TMEM lanes 32 (w % 4) .. +31 (its rows)
   // and SPAN columns starting at (w / 4) SPAN.  Its first PRE columns of C
@@ -368,17 +376,17 @@ static EncodeTiled encode_fn() {
 }
 
 // 2-D FP32 map: inner dimension `inner` (contiguous), outer `outer`, row
-// pitch `pitch` elements, box 32 x box_outer, 128-byte swizzle.
+// pitch `pitch` elements, box BK x box_outer, swizzle of BK * 4 bytes.
 static bool make_map(CUtensorMap* m, const float* base, uint64_t inner, uint64_t outer, uint64_t pitch,
                      uint32_t box_outer) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {inner, outer};
   cuuint64_t strides[1] = {pitch * 4};
-  cuuint32_t box[2] = {32, box_outer};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, box_outer};
   cuuint32_t es[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, tc::BK == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 

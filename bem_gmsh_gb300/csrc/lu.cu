@@ -17,39 +17,79 @@
 
 #include "bem_lu.h"
 #include "bem_prof.h"
+#include "df32.cuh"
 
 namespace bem {
 
 // ---------------------------------------------------------------------------
 // equilibration + FP32 copy with identity padding
 // ---------------------------------------------------------------------------
-__global__ void k_colscale(const double* __restrict__ A, int64_t lda, int N, double* __restrict__ cs) {
-  const int j = blockIdx.x;
-  if (j >= N) return;
-  const double* col = A + (size_t)j * lda;
-  double m = 0.0;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) m = fmax(m, fabs(col[i]));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ double s[32];
-  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, s[w]);
-    cs[j] = (r > 0.0 && r < INFINITY) ? 1.0 / r : 1.0;
+// One CTA per column of the padded matrix: the column's max |a| (first
+// pass, from HBM), the power-of-two column scale cs[j] = 2^s with
+// max |a| 2^s in [0.5, 1), then the scaled FP32 column (second pass, the
+// column's 8 N bytes are still in L2).  Padding columns and rows get the
+// identity.  HBM traffic: the FP64 matrix once, the FP32 copy once.
+// Everything runs on the integer pipes (GB300's FP64 pipe is a small
+// fraction of its FP32 rate): the max compares |a| as bit patterns (for
+// non-negative IEEE doubles the order of the patterns is the order of the
+// values), and the scaled conversion adds s to the exponent field and rounds
+// the 52-bit fraction to 23 bits to nearest, ties to even -- exactly
+// (float)(a * 2^s).  Values whose result leaves the normal FP32 range (not
+// met by a scaled column other than for zeros) take the FP64 instructions
+// (df::scale_to_f32).
+__global__ void __launch_bounds__(512) k_equilibrate(const double* __restrict__ A, int64_t lda, int N, int Npad,
+                                                     double* __restrict__ cs, float* __restrict__ A32,
+                                                     int64_t ld32) {
+  const int j = blockIdx.x, t = threadIdx.x;
+  float* out = A32 + (size_t)j * ld32;
+  if (j >= N) {
+    for (int i = t; i < Npad; i += blockDim.x) out[i] = (i == j) ? 1.f : 0.f;
+    return;
   }
-}
-
-// A32[i, j] = A[i, j] * cs[j] for i, j < N; identity on the padding.
-__global__ void k_scale_convert(const double* __restrict__ A, int64_t lda, int N, int Npad,
-                                const double* __restrict__ cs, float* __restrict__ A32, int64_t ld32) {
-  const int j = blockIdx.y;
-  const double s = j < N ? cs[j] : 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Npad; i += gridDim.x * blockDim.x) {
-    float v;
-    if (i < N && j < N) v = (float)(A[i + (size_t)j * lda] * s);
-    else v = (i == j) ? 1.f : 0.f;
-    A32[i + (size_t)j * ld32] = v;
+  const unsigned long long* col = (const unsigned long long*)(A + (size_t)j * lda);
+  constexpr unsigned long long ABS = 0x7FFFFFFFFFFFFFFFull;
+  // 16 independent loads in flight per thread and round
+  constexpr int V = 16;
+  unsigned long long mx = 0;
+  for (int base = 0; base < N; base += V * 512) {
+    unsigned long long v[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int i = base + q * 512 + t;
+      v[q] = i < N ? col[i] : 0ull;
+    }
+#pragma unroll
+    for (int q = 0; q < V; ++q) mx = max(mx, v[q] & ABS);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  __shared__ unsigned long long sw[16];
+  __shared__ int ssh;
+  if ((t & 31) == 0) sw[t >> 5] = mx;
+  __syncthreads();
+  if (t == 0) {
+    unsigned long long r = 0;
+    for (int w = 0; w < 16; ++w) r = max(r, sw[w]);
+    const int ex = (int)(r >> 52);
+    // zero, subnormal-only, inf or NaN columns keep scale 1
+    int sh = (ex == 0 || ex == 0x7FF) ? 0 : 1022 - ex;
+    if (sh < -1022) sh = -1022;
+    ssh = sh;
+    cs[j] = __longlong_as_double((long long)((unsigned long long)(1023 + sh) << 52));
+  }
+  __syncthreads();
+  const int sh = ssh;
+  for (int base = 0; base < Npad; base += V * 512) {
+    unsigned long long v[V];
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int i = base + q * 512 + t;
+      v[q] = i < N ? col[i] : 0ull;
+    }
+#pragma unroll
+    for (int q = 0; q < V; ++q) {
+      const int i = base + q * 512 + t;
+      if (i < Npad) out[i] = df::scale_to_f32(__longlong_as_double((long long)v[q]), sh);
+    }
   }
 }
 
@@ -688,10 +728,8 @@ __global__ void k_from_f32_scale(const float* __restrict__ y, const double* __re
 void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, float* A32, int64_t ld32,
                 cudaStream_t st) {
   KScope ks(st, KC_LU_PREP);
-  count_launches(2);
-  k_colscale<<<N, 256, 0, st>>>(A64, lda, N, cs);
-  dim3 grid((Npad + 255) / 256, Npad);
-  k_scale_convert<<<grid, 256, 0, st>>>(A64, lda, N, Npad, cs, A32, ld32);
+  count_launches(1);
+  k_equilibrate<<<Npad, 512, 0, st>>>(A64, lda, N, Npad, cs, A32, ld32);
 }
 
 // ---------------------------------------------------------------------------
@@ -1103,27 +1141,30 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Linv, 
 }
 
 // ---------------------------------------------------------------------------
-// Thin look-ahead updates of one LU step in FP32 on the CUDA cores, both in
-// one launch: block column k+1 (C: rem x 128) and block row k+1 (C: 128 x
-// rem-128) get C -= L21 U12 with K = 128.  64 x 64 tiles, operands staged by
-// cp.async, 4 x 4 register tiles; a 1-D grid lists the tiles of both parts.
+// Thin look-ahead updates of one LU step in FP32 on the CUDA cores: block
+// column k+1 (C: rem x 128) and block row k+1 (C: 128 x rem-128) get
+// C -= L21 U12 with K = 128.  64 x 64 tiles, operands staged by cp.async,
+// 4 x 4 register tiles; a 1-D grid lists the tiles.  The column part covers
+// rows [ro, ro + M0) of the block column; the row part is included when
+// with_row is set (the look-ahead runs the diagonal block, ro = 0 and
+// M0 = 128, ahead of the rest).
 // ---------------------------------------------------------------------------
 constexpr int TT = 64;
 constexpr int TPLD = TT + 4;      // staged L: [q][r]
 constexpr int TQLD = LU_NB + 4;   // staged U: [c][q]
 constexpr int THIN_SMEM = (int)sizeof(float) * (LU_NB * TPLD + TT * TQLD);
 
-__global__ void __launch_bounds__(256) k_thin_update(float* A, int64_t ld, int kk, int rem) {
+__global__ void __launch_bounds__(256) k_thin_update(float* A, int64_t ld, int kk, int rem, int ro, int M0) {
   extern __shared__ __align__(16) float tsm[];
   float* Ps = tsm;                  // Ps[q * TPLD + r] = L21(m0 + r, q)
   float* Qs = tsm + LU_NB * TPLD;   // Qs[c * TQLD + q] = U12(q, n0 + c)
   const int t = threadIdx.x;
-  const int ncol = (rem / TT) * (LU_NB / TT);
+  const int ncol = (M0 / TT) * (LU_NB / TT);
   int tile = blockIdx.x, z = 0;
   if (tile >= ncol) { tile -= ncol; z = 1; }
-  const int M = z == 0 ? rem : LU_NB;
+  const int M = z == 0 ? M0 : LU_NB;
   const int mt = M / TT;
-  const int m0 = (tile % mt) * TT, n0 = (tile / mt) * TT;
+  const int m0 = (tile % mt) * TT + (z == 0 ? ro : 0), n0 = (tile / mt) * TT;
   const int co = z == 0 ? 0 : LU_NB;
   const size_t r_abs = (size_t)kk + LU_NB + m0, c_abs = (size_t)kk + LU_NB + co + n0;
   float* C = A + r_abs + c_abs * ld;
@@ -1171,10 +1212,16 @@ __global__ void __launch_bounds__(256) k_thin_update(float* A, int64_t ld, int k
   }
 }
 
-static void thin_update(float* A, int64_t ld, int k, int rem, cudaStream_t st) {
-  const int tiles = (rem / TT) * (LU_NB / TT) + (LU_NB / TT) * ((rem - LU_NB) / TT);
-  k_thin_update<<<tiles, 256, THIN_SMEM, st>>>(A, ld, k * LU_NB, rem);
+// rows [ro, ro + M0) of block column k+1, plus block row k+1 if with_row
+static void thin_part(float* A, int64_t ld, int k, int rem, int ro, int M0, bool with_row, cudaStream_t st) {
+  const int tiles = (M0 / TT) * (LU_NB / TT) + (with_row ? (LU_NB / TT) * ((rem - LU_NB) / TT) : 0);
+  if (tiles <= 0) return;
+  KScope kt(st, KC_LU_THIN);
+  k_thin_update<<<tiles, 256, THIN_SMEM, st>>>(A, ld, k * LU_NB, rem, ro, M0);
   count_launches(1);
+}
+static void thin_update(float* A, int64_t ld, int k, int rem, cudaStream_t st) {
+  thin_part(A, ld, k, rem, 0, rem, true, st);
 }
 
 static void lu_attrs_once();
@@ -1194,21 +1241,33 @@ static void lu_attrs_once() {
   cudaFuncSetAttribute(k_thin_update, cudaFuncAttributeMaxDynamicSharedMemorySize, THIN_SMEM);
 }
 
-// diagonal block k and its two panels: U12 = Linv A12, L21 = A21 Uinv
-static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, int k,
-                            cudaStream_t st) {
-  const size_t kk = (size_t)k * LU_NB;
-  const int rem = Npad - (int)kk - LU_NB;
+// diagonal block k
+static void diag_block(float* A, int64_t ld, float* Dinv, int* info, int k, cudaStream_t st) {
+  KScope kd(st, KC_LU_DIAG);
   k_diag_factor_tiled<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, Dinv, info);
   count_launches(1);
+}
+
+// the two panels of diagonal block k: U12 = Linv A12, L21 = A21 Uinv
+static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st) {
+  const size_t kk = (size_t)k * LU_NB;
+  const int rem = Npad - (int)kk - LU_NB;
   if (rem <= 0) return;
   const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
   const float* Ui = Li + LU_NB * LU_NB;
   float* A12 = A + kk + (kk + LU_NB) * ld;
   float* A21 = A + (kk + LU_NB) + kk * ld;
-  (void)x3;  // panels in full FP32 on the CUDA cores
+  KScope kp(st, KC_LU_PANELS);
   k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(Li, A12, Ui, A21, ld);
   count_launches(1);
+}
+
+// diagonal block k and its two panels (panels in full FP32 on the CUDA cores)
+static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, int k,
+                            cudaStream_t st) {
+  (void)x3;
+  diag_block(A, ld, Dinv, info, k, st);
+  panels(A, ld, Npad, Dinv, k, st);
 }
 
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,

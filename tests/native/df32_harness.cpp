@@ -35,3 +35,12 @@ void df_diff_batch(const double* xn, const double* xs, int n, double* out) {
 }
 
 }
+
+extern "C" {
+
+// (float)(v * 2^s) on the integer path of the equilibration kernel
+void df_scale_to_f32_batch(const double* v, const int* s, int n, float* out) {
+  for (int i = 0; i < n; ++i) out[i] = df::scale_to_f32(v[i], s[i]);
+}
+
+}

@@ -29,6 +29,7 @@ def h():
     for nm in ("df_div_batch", "df_mul_batch", "df_diff_batch"):
         getattr(L, nm).argtypes = [P, P, ctypes.c_int, P]
     L.df_to_double_batch.argtypes = [F, F, ctypes.c_int, P]
+    L.df_scale_to_f32_batch.argtypes = [P, ctypes.POINTER(ctypes.c_int), ctypes.c_int, F]
     return L
 
 
@@ -105,3 +106,24 @@ def test_to_double_rounding(h):
     # within one double ulp of the exact sum (round half away at the last bit)
     ulp = np.spacing(np.abs(out))
     assert np.all(np.abs(out.astype(np.longdouble) - exact) <= ulp.astype(np.longdouble))
+
+
+def test_scale_to_f32_matches_scaled_conversion(h):
+    """The equilibration's integer conversion equals (float)(v * 2^s) bit for
+    bit: random magnitudes, exact ties (even and odd), zeros, values whose
+    result leaves the FP32 range."""
+    rng = np.random.default_rng(11)
+    n = 200000
+    v = rng.standard_normal(n) * 10.0 ** rng.uniform(-12, 12, n)
+    s = rng.integers(-60, 60, n).astype(np.int32)
+    # ties: 24 significant bits then exactly half an FP32 ulp
+    m = rng.integers(1 << 23, 1 << 24, 4000).astype(np.float64)
+    ties = (m + 0.5) * 2.0 ** rng.integers(-30, 30, 4000)
+    v = np.concatenate([v, ties, -ties, [0.0, -0.0, 1e-300, -1e300, 3.4e38, 1e-45]])
+    s = np.concatenate([s, np.zeros(8000, np.int32), np.array([0, 0, 900, -900, 1, 0], np.int32)])
+    out = np.empty(len(v), np.float32)
+    h.df_scale_to_f32_batch(_p(v), s.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(v),
+                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    with np.errstate(over="ignore"):  # the 1e300 case overflows to -inf on purpose
+        ref = (v * np.ldexp(1.0, s)).astype(np.float32)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
