@@ -156,7 +156,11 @@ __device__ __forceinline__ bool box_far(float xh, float xl, float yh, float yl, 
 }
 
 // Possibly-near (point, element) pairs into the pair list: one thread per
-// point, the CTA's 256 elements staged in shared memory.
+// point, the CTA's 256 elements staged in shared memory.  Each warp first
+// tests an element against the bounding box of its 32 points with the same
+// operations: IEEE subtraction is monotonic, so a box distance above the
+// limit means every point of the warp is far by the per-point test, and the
+// 32 point tests are skipped.
 __global__ void __launch_bounds__(256) near_classify_kernel(int nt, int ne, const float4* __restrict__ rows,
                                                             const ElemRec* __restrict__ elems,
                                                             int* pair_count, int2* pairs, int pair_cap) {
@@ -169,8 +173,20 @@ __global__ void __launch_bounds__(256) near_classify_kernel(int nt, int ne, cons
   const bool valid = i < nt;
   const float4 r = rows[valid ? i : nt - 1];
   const int lane = threadIdx.x & 31;
+  const float x = __fadd_rn(r.x, r.y), y = __fadd_rn(r.z, r.w);
+  float bx0 = x, bx1 = x, by0 = y, by1 = y;
+  for (int o = 16; o > 0; o >>= 1) {
+    bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+    bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+    by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+    by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+  }
   for (int el = 0; el < nel; ++el) {
-    const bool need = valid && !box_far(r.x, r.y, r.z, r.w, s_e[el]);
+    const ElemRec E = s_e[el];
+    const float dx = fmaxf(fmaxf(__fsub_rn(E.lox, bx1), __fsub_rn(bx0, E.hix)), 0.f);
+    const float dy = fmaxf(fmaxf(__fsub_rn(E.loy, by1), __fsub_rn(by0, E.hiy)), 0.f);
+    if (__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) > E.lim2) continue;  // warp-uniform
+    const bool need = valid && !box_far(r.x, r.y, r.z, r.w, E);
     const unsigned m = __ballot_sync(0xffffffffu, need);
     if (m) {
       const int leader = __ffs(m) - 1;

@@ -9,9 +9,9 @@
 // 1-7 the polyharmonic splines R, R^2 log(R+e), R^3, R^4 log(R+e), R^5,
 // R^6 log(R+e), R^7, kind 10 the fundamental solution.  Entries with
 // i == j or R^2 <= eps^2 stay zero.  Outputs column-major (Julia layout).
-// Each thread writes 16 bytes of one column (2 FP64 or 4 FP32 rows), so a
-// warp stores a contiguous 512-byte segment: the kernel is bound by the HBM
-// write of F and D.
+// Each thread writes 16 bytes (2 FP64 or 4 FP32 rows) of each of its CTA's
+// 32 columns, so a warp stores contiguous 512-byte segments: the FP32 kernel
+// is bound by the HBM write of F and D, the FP64 one by FP64 issue.
 #include <cfloat>
 #include <cmath>
 
@@ -35,85 +35,119 @@ __device__ __forceinline__ T dibem_phi(int kind, T R, T kcond, T epsa) {
   }
 }
 
+// columns per CTA: the CTA's row and column coordinates are converted to T
+// once (on GB300 the FP64-to-FP32 conversion runs on the slow FP64 pipe)
+constexpr int JPC = 32;
+
 // Laplace: F, D (nt x nt)
 template <typename T>
-__global__ void dibem_laplace_kernel(int nt, const double* __restrict__ px, const double* __restrict__ py,
-                                     T kcond, int kind, T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
+__global__ void __launch_bounds__(128) dibem_laplace_kernel(int nt, const double* __restrict__ px,
+                                                            const double* __restrict__ py, T kcond, int kind,
+                                                            T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
   constexpr int RPT = 16 / sizeof(T);
-  const int j = blockIdx.y;
+  __shared__ T sx[JPC], sy[JPC];
+  const int j0 = blockIdx.y * JPC;
+  const int nj = min(JPC, nt - j0);
+  if ((int)threadIdx.x < nj) {
+    sx[threadIdx.x] = (T)px[j0 + threadIdx.x];
+    sy[threadIdx.x] = (T)py[j0 + threadIdx.x];
+  }
   const int i0 = (blockIdx.x * blockDim.x + threadIdx.x) * RPT;
-  if (i0 >= nt) return;
-  const T xj = (T)px[j], yj = (T)py[j];
-  const T inv2pi = T(1) / (T(2) * T(3.14159265358979323846));
-  T f[RPT], d[RPT];
+  T xi[RPT], yi[RPT];
 #pragma unroll
   for (int r = 0; r < RPT; ++r) {
-    const int i = i0 + r;
-    f[r] = T(0);
-    d[r] = T(0);
-    if (i < nt && i != j) {
-      const T rx = xj - (T)px[i], ry = yj - (T)py[i];
-      const T R2 = rx * rx + ry * ry;
-      if (R2 > eps2) {
-        const T R = sqrt(R2);
-        d[r] = -log(R) * inv2pi / kcond;
-        f[r] = dibem_phi<T>(kind, R, kcond, epsa);
-      }
-    }
+    const int i = min(i0 + r, nt - 1);
+    xi[r] = (T)px[i];
+    yi[r] = (T)py[i];
   }
-  T* Fc = F + i0 + (size_t)j * ldf;
-  T* Dc = D + i0 + (size_t)j * ldd;
+  __syncthreads();
+  if (i0 >= nt) return;
+  const T inv2pi = T(1) / (T(2) * T(3.14159265358979323846));
   const bool vec = (i0 + RPT <= nt) && ((ldf | ldd) % RPT == 0) && (((uintptr_t)F | (uintptr_t)D) % 16 == 0);
-  if (vec) {
-    if constexpr (sizeof(T) == 8) {
-      *(double2*)Fc = make_double2(f[0], f[1]);
-      *(double2*)Dc = make_double2(d[0], d[1]);
-    } else {
-      *(float4*)Fc = make_float4(f[0], f[1], f[2], f[3]);
-      *(float4*)Dc = make_float4(d[0], d[1], d[2], d[3]);
-    }
-  } else {
+  for (int jj = 0; jj < nj; ++jj) {
+    const int j = j0 + jj;
+    const T xj = sx[jj], yj = sy[jj];
+    T f[RPT], d[RPT];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r)
-      if (i0 + r < nt) {
-        Fc[r] = f[r];
-        Dc[r] = d[r];
+    for (int r = 0; r < RPT; ++r) {
+      const int i = i0 + r;
+      f[r] = T(0);
+      d[r] = T(0);
+      if (i < nt && i != j) {
+        const T rx = xj - xi[r], ry = yj - yi[r];
+        const T R2 = rx * rx + ry * ry;
+        if (R2 > eps2) {
+          const T R = sqrt(R2);
+          d[r] = -log(R) * inv2pi / kcond;
+          f[r] = dibem_phi<T>(kind, R, kcond, epsa);
+        }
       }
+    }
+    T* Fc = F + i0 + (size_t)j * ldf;
+    T* Dc = D + i0 + (size_t)j * ldd;
+    if (vec) {
+      if constexpr (sizeof(T) == 8) {
+        *(double2*)Fc = make_double2(f[0], f[1]);
+        *(double2*)Dc = make_double2(d[0], d[1]);
+      } else {
+        *(float4*)Fc = make_float4(f[0], f[1], f[2], f[3]);
+        *(float4*)Dc = make_float4(d[0], d[1], d[2], d[3]);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < RPT; ++r)
+        if (i0 + r < nt) {
+          Fc[r] = f[r];
+          Dc[r] = d[r];
+        }
+    }
   }
 }
 
 // Kelvin: F (nt x nt), D (2nt x 2nt, node-major 2x2 blocks u11 u12; u12 u22)
 template <typename T>
-__global__ void dibem_kelvin_kernel(int nt, const double* __restrict__ px, const double* __restrict__ py,
-                                    T mu, T nu, int kind, T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
-  const int j = blockIdx.y;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nt) return;
-  T f = T(0), u11 = T(0), u12 = T(0), u22 = T(0);
-  if (i != j) {
-    const T rx = (T)px[j] - (T)px[i], ry = (T)py[j] - (T)py[i];
-    const T R2 = rx * rx + ry * ry;
-    if (R2 > eps2) {
-      const T R = sqrt(R2);
-      f = dibem_phi<T>(kind, R, T(1), epsa);
-      // U of the 2-D Kelvin solution (`_kelvin2d_UT`, Elasticity/Fundamental.jl)
-      const T pi = T(3.14159265358979323846);
-      const T dr1 = rx / R, dr2 = ry / R;
-      const T prod1 = T(4) * pi * (T(1) - nu);
-      const T prod2 = (T(3) - T(4) * nu) * (-log(R));
-      const T base = T(2) * prod1 * mu;
-      u11 = (prod2 + dr1 * dr1) / base;
-      u12 = (dr1 * dr2) / base;
-      u22 = (prod2 + dr2 * dr2) / base;
-    }
+__global__ void __launch_bounds__(128) dibem_kelvin_kernel(int nt, const double* __restrict__ px,
+                                                           const double* __restrict__ py, T mu, T nu, int kind,
+                                                           T epsa, T eps2, T* F, int64_t ldf, T* D, int64_t ldd) {
+  __shared__ T sx[JPC], sy[JPC];
+  const int j0 = blockIdx.y * JPC;
+  const int nj = min(JPC, nt - j0);
+  if ((int)threadIdx.x < nj) {
+    sx[threadIdx.x] = (T)px[j0 + threadIdx.x];
+    sy[threadIdx.x] = (T)py[j0 + threadIdx.x];
   }
-  F[i + (size_t)j * ldf] = f;
-  T* c0 = D + 2 * (size_t)i + (size_t)(2 * j) * ldd;
-  T* c1 = c0 + ldd;
-  c0[0] = u11;
-  c0[1] = u12;
-  c1[0] = u12;
-  c1[1] = u22;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const T xi = (T)px[min(i, nt - 1)], yi = (T)py[min(i, nt - 1)];
+  __syncthreads();
+  if (i >= nt) return;
+  const T pi = T(3.14159265358979323846);
+  const T prod1 = T(4) * pi * (T(1) - nu);
+  const T base = T(2) * prod1 * mu;
+  for (int jj = 0; jj < nj; ++jj) {
+    const int j = j0 + jj;
+    T f = T(0), u11 = T(0), u12 = T(0), u22 = T(0);
+    if (i != j) {
+      const T rx = sx[jj] - xi, ry = sy[jj] - yi;
+      const T R2 = rx * rx + ry * ry;
+      if (R2 > eps2) {
+        const T R = sqrt(R2);
+        f = dibem_phi<T>(kind, R, T(1), epsa);
+        // U of the 2-D Kelvin solution (`_kelvin2d_UT`, Elasticity/Fundamental.jl)
+        const T dr1 = rx / R, dr2 = ry / R;
+        const T prod2 = (T(3) - T(4) * nu) * (-log(R));
+        u11 = (prod2 + dr1 * dr1) / base;
+        u12 = (dr1 * dr2) / base;
+        u22 = (prod2 + dr2 * dr2) / base;
+      }
+    }
+    F[i + (size_t)j * ldf] = f;
+    T* c0 = D + 2 * (size_t)i + (size_t)(2 * j) * ldd;
+    T* c1 = c0 + ldd;
+    c0[0] = u11;
+    c0[1] = u12;
+    c1[0] = u12;
+    c1[1] = u22;
+  }
 }
 
 }  // namespace
@@ -156,7 +190,7 @@ extern "C" int bem_dibem_fd2d(bem_ctx* c, int nt, const double* px, const double
   }
   if (kind == 0) {
     const int rpt = (int)(16 / esz);
-    dim3 grid((unsigned)((n + 128 * rpt - 1) / (128 * rpt)), (unsigned)n);
+    dim3 grid((unsigned)((n + 128 * rpt - 1) / (128 * rpt)), (unsigned)((n + JPC - 1) / JPC));
     if (dtype == BEM_F64)
       dibem_laplace_kernel<double><<<grid, 128, 0, c->stream>>>(nt, dx, dy, prm0, rbf, epsa, DBL_EPSILON * DBL_EPSILON,
                                                                (double*)dF, lf, (double*)dD, lD);
@@ -164,7 +198,7 @@ extern "C" int bem_dibem_fd2d(bem_ctx* c, int nt, const double* px, const double
       dibem_laplace_kernel<float><<<grid, 128, 0, c->stream>>>(nt, dx, dy, (float)prm0, rbf, (float)epsa,
                                                               FLT_EPSILON * FLT_EPSILON, (float*)dF, lf, (float*)dD, lD);
   } else {
-    dim3 grid((unsigned)((n + 127) / 128), (unsigned)n);
+    dim3 grid((unsigned)((n + 127) / 128), (unsigned)((n + JPC - 1) / JPC));
     if (dtype == BEM_F64)
       dibem_kelvin_kernel<double><<<grid, 128, 0, c->stream>>>(nt, dx, dy, prm0, prm1, rbf, epsa,
                                                               DBL_EPSILON * DBL_EPSILON, (double*)dF, lf, (double*)dD, lD);

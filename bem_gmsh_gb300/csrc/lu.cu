@@ -494,45 +494,45 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 // triangular sweep to the block solved just before it.  With
 //   z_b = D_b (r_b - sum over the other solved blocks),  y_b = z_b - M_b y_prev
 // the sweep's dependent step is one 128 x 128 product; z_b is formed while
-// the previous block is still being solved.  One CTA per (block, side),
-// 8 x 8 outputs per thread.
-constexpr int CPL_LD = LU_NB + 1;
+// the previous block is still being solved.  One CTA per (block, side,
+// 64 x 64 quadrant), 4 x 4 outputs per thread.
+constexpr int CPL_LD = 64 + 4;
 constexpr int CPL_SMEM = (int)sizeof(float) * 2 * LU_NB * CPL_LD;
 
 __global__ void __launch_bounds__(256) k_lu_couplings(const float* __restrict__ A, int64_t ld, int K,
                                                       const float* __restrict__ Dinv, float* __restrict__ Mc) {
-  extern __shared__ float cs_[];
-  const int b = blockIdx.x, side = blockIdx.y, t = threadIdx.x;
+  extern __shared__ __align__(16) float cs_[];
+  const int b = blockIdx.x, side = blockIdx.y, quad = blockIdx.z, t = threadIdx.x;
   if (side == 0 ? b == 0 : b == K - 1) return;
-  float* P = cs_;                  // D_b, [col][row]
-  float* Q = cs_ + LU_NB * CPL_LD;  // coupling block of A, [col][row]
+  const int qr = (quad & 1) * 64, qc = (quad >> 1) * 64;
+  float* P = cs_;                   // D_b rows [qr, qr + 64): P[k][r]
+  float* Q = cs_ + LU_NB * CPL_LD;  // coupling block columns [qc, qc + 64): Q[k][c]
   const float* Pg = Dinv + (size_t)b * 2 * LU_NB * LU_NB + (side ? LU_NB * LU_NB : 0);
   const int qb = side ? b + 1 : b - 1;
   const float* Qg = A + (size_t)b * LU_NB + (size_t)qb * LU_NB * ld;
-  for (int idx = t; idx < LU_NB * LU_NB; idx += 256) {
-    const int r = idx & (LU_NB - 1), c = idx >> 7;
-    P[c * CPL_LD + r] = Pg[r + (size_t)c * LU_NB];
-    Q[c * CPL_LD + r] = Qg[r + (size_t)c * ld];
+  for (int idx = t; idx < LU_NB * 64; idx += 256) {
+    const int r = idx & 63, k = idx >> 6;
+    P[k * CPL_LD + r] = Pg[qr + r + (size_t)k * LU_NB];  // D_b(qr + r, k), column-major
+    const int k2 = idx & (LU_NB - 1), c = idx >> 7;
+    Q[k2 * CPL_LD + c] = Qg[k2 + (size_t)(qc + c) * ld];  // block(k2, qc + c), coalesced reads
   }
   __syncthreads();
-  const int r0 = (t >> 4) * 8, c0 = (t & 15) * 8;
-  float acc[8][8] = {};
+  const int r0 = 4 * (t & 15), c0 = 4 * (t >> 4);
+  float acc[4][4] = {};
+#pragma unroll 4
   for (int k = 0; k < LU_NB; ++k) {
-    float a[8], q[8];
+    const float4 a = *(const float4*)&P[k * CPL_LD + r0];
+    const float4 q = *(const float4*)&Q[k * CPL_LD + c0];
+    const float av[4] = {a.x, a.y, a.z, a.w}, qv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = P[k * CPL_LD + r0 + i];
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) q[j] = Q[(c0 + j) * CPL_LD + k];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], q[j], acc[i][j]);
+      for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], qv[j], acc[i][j]);
   }
   float* Mo = Mc + (size_t)(2 * b + side) * LU_NB * LU_NB;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
-#pragma unroll
-    for (int i = 0; i < 8; ++i) Mo[(size_t)(c0 + j) * LU_NB + r0 + i] = acc[i][j];
+  for (int j = 0; j < 4; ++j)
+    *(float4*)&Mo[(size_t)(qc + c0 + j) * LU_NB + qr + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
 }
 
 template <bool UPPER>
@@ -1371,7 +1371,7 @@ void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float
   if (K < 2) return;
   KScope ks(st, KC_TRSV);
   count_launches(1);
-  k_lu_couplings<<<dim3(K, 2), 256, CPL_SMEM, st>>>(A, ld, K, Dinv, Mc);
+  k_lu_couplings<<<dim3(K, 2, 4), 256, CPL_SMEM, st>>>(A, ld, K, Dinv, Mc);
 }
 
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
