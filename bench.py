@@ -114,12 +114,12 @@ def cpu_reference(dad_factory, steps, warmup, npg):
     return ts, x
 
 
-# DRAM traffic of one bulk trailing update (k_gemm_tc) at full C2 size, from
-# profiles/k_gemm_tc_bulk_update_c2_traffic.md: LU step 10 (trailing block
-# 6784^2), dram__bytes_read 198152192 B + dram__bytes_write 123085824 B for
-# 8 * 6784^2 = 368181248 algorithmic bytes.
-GEMM_TRAFFIC_CAPTURE = {"launch": "LU step 10 (trailing block 6784^2)", "read_bytes": 198152192,
-                        "write_bytes": 123085824, "algorithmic_bytes": 8 * 6784 ** 2}
+# DRAM traffic of one bulk trailing update (k_gemm_tc) at the C2 trailing size,
+# from one ncu capture of the update timed alone (bem_selftest which = 3,
+# n = 8192, trailing block 8064^2): dram__bytes_read 276831744 B +
+# dram__bytes_write 199586048 B for 8 * 8064^2 = 520224768 algorithmic bytes.
+GEMM_TRAFFIC_CAPTURE = {"launch": "bulk update alone, trailing block 8064^2", "read_bytes": 276831744,
+                        "write_bytes": 199586048, "algorithmic_bytes": 8 * 8064 ** 2}
 
 
 def extra_configs(ctx):
@@ -405,7 +405,7 @@ def main():
         pk = hbm if bound == "hbm" else bf16
         classes[k] = {"bound": bound, "achieved": ach, "unit": unit, "peak": pk, "frac": ach / pk,
                       "ms_per_step": ms_k / prof_steps, "note": note}
-    # the dominant kernel of the launch list (profiles/) is the tcgen05 GEMM
+    # the dominant kernel of the ncu launch list is the tcgen05 GEMM
     # of the bulk trailing update; its class is lu_trail
     dom = "lu_trail" if "lu_trail" in classes else max(classes, key=lambda k: classes[k]["ms_per_step"])
     roof = dict(classes[dom])
