@@ -150,6 +150,13 @@ bool bem_ctx::lookahead_ready(int k) {
     }
     if (cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming) != cudaSuccess) return false;
   }
+  if (!inv_stream) {
+    if (cudaStreamCreateWithFlags(&inv_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      inv_stream = nullptr;
+      return false;
+    }
+    if (cudaEventCreateWithFlags(&inv_done, cudaEventDisableTiming) != cudaSuccess) return false;
+  }
   while ((int)events.size() < 2 * k) {
     cudaEvent_t e;
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
@@ -201,6 +208,8 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   if (c->asm_stream2) cudaStreamDestroy(c->asm_stream2);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
+  if (c->inv_done) cudaEventDestroy(c->inv_done);
+  if (c->inv_stream) cudaStreamDestroy(c->inv_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return BEM_OK;

@@ -43,6 +43,9 @@ struct bem_ctx {
   cudaStream_t la_stream = nullptr;
   cudaEvent_t fork_event = nullptr;
   std::vector<cudaEvent_t> events;
+  // third stream of the lookahead LU (diagonal-block inverses) and its end
+  cudaStream_t inv_stream = nullptr;
+  cudaEvent_t inv_done = nullptr;
   // Ensures 2*k events and the lookahead stream; false on failure.
   bool lookahead_ready(int k);
 

@@ -4,27 +4,33 @@
 #include <cuda_runtime.h>
 
 #define LU_NB 128  // LU block size (rows/columns of a diagonal block)
+#define LU_SB 16   // sub-block of the diagonal factorization and of the panel solves
+// floats per diagonal block of the 16 x 16 sub-block inverses (L^{-1}, U^{-1})
+#define LU_SI (2 * (LU_NB / LU_SB) * LU_SB * LU_SB)
 
 namespace bem {
 
-// cs[j] = 1 / max_i |A[i, j]|; A32 = A * diag(cs) in FP32, identity padding
-// up to Npad (a multiple of LU_NB).
+// cs[j] = 2^s_j with max_i |A[i, j]| 2^s_j in [0.5, 1); A32 = A * diag(cs)
+// rounded to FP32, identity padding up to Npad (a multiple of LU_NB).
 void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, float* A32,
                 int64_t ld32, cudaStream_t st);
 // In-place blocked LU without pivoting of the Npad x Npad FP32 matrix.
-// Dinv receives, per diagonal block, the inverses of its unit-lower and
-// upper triangles (2 x LU_NB^2 floats per block).  info: first block with a
-// vanishing pivot (1-based), untouched otherwise.  x3: 3xTF32 updates.
+// Dinv (lu_dinv_floats(K) floats) receives, per diagonal block, the inverses
+// of its unit-lower and upper triangles (2 x LU_NB^2 floats per block), and
+// after all blocks the 16 x 16 sub-block inverses (LU_SI floats per block).
+// info: first block with a vanishing pivot (1-based), untouched otherwise.
+// x3: 3xTF32 updates.
+inline size_t lu_dinv_floats(int K) { return (size_t)K * (2 * LU_NB * LU_NB + LU_SI); }
 struct TcPlan;
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
               const TcPlan* tc = nullptr, int* err = nullptr);
+// M_b couplings of the triangular sweeps (Mc: K * 2 * 128^2 floats), after
+// the factorization
+void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float* Mc, cudaStream_t st);
 // out <- U^{-1} L^{-1} r on padded FP32 vectors.  tmp: Npad floats (the
 // forward result); tags: 2 Npad words of (epoch, value) scratch, zeroed
 // before the first call; epoch: > 0 and different in every call on the same
 // tags; err: timeout flag.  r may be clobbered.  Returns 0 or a CUDA error.
-// M_b couplings of the triangular sweeps (Mc: K * 2 * 128^2 floats), after
-// the factorization
-void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float* Mc, cudaStream_t st);
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st);
 
@@ -42,7 +48,8 @@ void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStre
 void gemm_tile128(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc,
                   int M, int N, float alpha, float beta, int x3, cudaStream_t st);
 
-void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, int* info, cudaStream_t st);
+void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float* SI, int* info,
+                   cudaStream_t st);
 
 // tcgen05 trailing update (gemm_tc.cu).  The plan holds the TMA maps of the
 // transposed L panel, its lo part, the matrix (U panel) and the U lo part.
@@ -67,6 +74,6 @@ void tc_split(const TcPlan& p, int k, cudaStream_t st);
 int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st);
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        const TcPlan* tc, int* err);
+                        cudaStream_t iv, cudaEvent_t ivdone, const TcPlan* tc, int* err);
 
 }  // namespace bem

@@ -733,32 +733,30 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 }
 
 // ---------------------------------------------------------------------------
-// Factorization of a 128 x 128 diagonal block (no pivoting) with the
-// inverses of its unit-lower and upper triangles, all in shared memory
-// (column-major, ld 132 so that 4 consecutive rows are one 16-byte load).
-// For each 16-wide panel p (jb = 16 p):
+// Factorization of a 128 x 128 diagonal block (no pivoting) in shared memory
+// (column-major, ld 132 so that 4 consecutive rows are one 16-byte load),
+// with the inverses of its eight 16 x 16 diagonal sub-blocks of L and U, the
+// inputs of the blocked triangular panel solves (k_panels).  For each
+// 16-wide panel p (jb = 16 p):
 //   A  warps 0-3 factor the panel: every warp holds its own copy of the 16
 //      pivot rows (lane r < 16: row jb + r) and updates them identically, and
 //      32 rows below them (lane: row jb + 16 + 32 w + lane), so no barrier
 //      is needed between columns; the pivot row of each column reaches the
 //      lanes through a double-buffered row in shared memory.  Warp 1 then
 //      inverts the unit-lower 16 x 16 block (one column per lane).
-//      Meanwhile warps 4-15 form the products for the new block row of
-//      L^{-1} and block column of U^{-1}:
-//        T_L = L[p, <p] Linv[<p, <p],   T_U = Uinv[<p, <p] U[<p, p].
-//   B  block row of U: U[p, >p] = Linv_pp A[p, >p]; Linv[p, <p] = -Linv_pp T_L;
-//      warp 12 inverts the upper 16 x 16 block.  Column block p of L\U and
-//      block row p of L^{-1} are final and are written out.
-//   C  Uinv[<p, p] = -T_U Uinv_pp, and the trailing update A22 -= L21 U12 on
-//      4 x 4 register tiles; block column p of U^{-1} is written out.
-// 24 block barriers in all.  A and ld must allow 16-byte accesses
-// (ld % 4 == 0, 16-byte aligned A).
+//   B  block row of U: U[p, >p] = Linv_pp A[p, >p]; warp 4 inverts the upper
+//      16 x 16 block.  Column block p of L\U and both sub-block inverses are
+//      final and are written out.
+//   C  the trailing update A22 -= L21 U12 on 4 x 4 register tiles.
+// 24 block barriers in all; 70 KB of shared memory, so the kernel starts
+// beside a bulk-update tile.  A and ld must allow 16-byte accesses (ld % 4 ==
+// 0, 16-byte aligned A).
 // ---------------------------------------------------------------------------
-constexpr int DB = 16;          // panel width
+constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
-// shared floats of the diagonal kernel: L\U, L^{-1}, U^{-1}, four double-
-// buffered pivot rows, the 16 x 16 scratch of the lower inverse
-constexpr int DIAG_SMEM = (int)sizeof(float) * (3 * LU_NB * TLD + 4 * 32 + 16 * 20);
+// shared floats of the diagonal kernel: L\U, four double-buffered pivot
+// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses
+constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 2 * DB * DB);
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -799,19 +797,18 @@ __device__ __forceinline__ float rcp_nr(float x) {
   return fmaf(r, fmaf(-x, r, 1.f), r);
 }
 
-__global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict__ A, int64_t ld, int k,
-                                                           float* __restrict__ Dinv, int* __restrict__ info) {
+__global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64_t ld, int k,
+                                                 float* __restrict__ SI, int* __restrict__ info) {
   extern __shared__ __align__(16) float dsm[];
-  float* S = dsm;                    // A -> L\U
-  float* Li = S + LU_NB * TLD;       // L^{-1}
-  float* Ui = Li + LU_NB * TLD;      // U^{-1}
-  float* rowbuf = Ui + LU_NB * TLD;  // [warp 0-3][2][16]
-  float* Ls = rowbuf + 4 * 32;       // 16 x 16 unit lower, column-major, ld 20
+  float* S = dsm;                       // A -> L\U
+  float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
+  float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
+  float* LiP = Ls + 16 * 20;            // Linv_pp, column-major, ld 16
+  float* UiP = LiP + DB * DB;           // Uinv_pp, column-major, ld 16
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
   float* Ab = A + off + off * ld;
-  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
-  float* Uo = Lo + LU_NB * LU_NB;
+  float* SIk = SI + (size_t)k * LU_SI;  // [p][Linv_pp 256, Uinv_pp 256]
   {
     // 8 float4 per thread, all loads in flight before the first store
     float4 v[8];
@@ -820,13 +817,10 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
       const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
       v[i] = __ldcg((const float4*)(Ab + r4 + (size_t)c * ld));
     }
-    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
       *(float4*)&S[c * TLD + r4] = v[i];
-      *(float4*)&Li[c * TLD + r4] = z;
-      *(float4*)&Ui[c * TLD + r4] = z;
     }
   }
   __syncthreads();
@@ -901,23 +895,7 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
         if (tv) {
 #pragma unroll
           for (int i4 = 0; i4 < DB; i4 += 4)
-            *(float4*)&Li[(jb + lane) * TLD + jb + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
-        }
-      }
-    } else if (jb > 0) {
-      // T_L (16 x jb) into Li[p, <p] and T_U (jb x 16) into Ui[<p, p], on
-      // 4 x 1 tiles
-      const int nL = 4 * jb, nU = jb * 4;
-      for (int idx = t - 128; idx < nL + nU; idx += 384) {
-        float acc[4][1] = {};
-        if (idx < nL) {
-          const int r0 = 4 * (idx & 3), c = idx >> 2;
-          tile_mm<1>(S + jb, Li, r0, c, c & ~3, jb, acc);
-          tile_store<1>(Li + jb, r0, c, acc);
-        } else {
-          const int iu = idx - nL, c = iu & 15, r0 = 4 * (iu >> 4);
-          tile_mm<1>(Ui, S + jb * TLD, r0, c, r0, jb, acc);
-          tile_store<1>(Ui + jb * TLD, r0, c, acc);
+            *(float4*)&LiP[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
         }
       }
     }
@@ -938,7 +916,7 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
         for (int q = 0; q < DB; ++q) {
 #pragma unroll
           for (int i4 = 0; i4 < DB; i4 += 4) {
-            const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
+            const float4 l = *(const float4*)&LiP[q * DB + i4];
             o[i4] = fmaf(l.x, v[q], o[i4]);
             o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
             o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
@@ -949,33 +927,7 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
         for (int q4 = 0; q4 < DB; q4 += 4)
           *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
       }
-    } else if (t < 256) {
-      const int c = t - 128;  // Linv[p, c] = -Linv_pp T_L[:, c]
-      if (c < jb) {
-        float v[DB], o[DB];
-#pragma unroll
-        for (int q4 = 0; q4 < DB; q4 += 4) {
-          const float4 a = *(const float4*)&Li[c * TLD + jb + q4];
-          v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
-        }
-#pragma unroll
-        for (int i = 0; i < DB; ++i) o[i] = 0.f;
-#pragma unroll
-        for (int q = 0; q < DB; ++q) {
-#pragma unroll
-          for (int i4 = 0; i4 < DB; i4 += 4) {
-            const float4 l = *(const float4*)&Li[(jb + q) * TLD + jb + i4];
-            o[i4] = fmaf(-l.x, v[q], o[i4]);
-            o[i4 + 1] = fmaf(-l.y, v[q], o[i4 + 1]);
-            o[i4 + 2] = fmaf(-l.z, v[q], o[i4 + 2]);
-            o[i4 + 3] = fmaf(-l.w, v[q], o[i4 + 3]);
-          }
-        }
-#pragma unroll
-        for (int q4 = 0; q4 < DB; q4 += 4)
-          *(float4*)&Li[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
-      }
-    } else if (warp == 12) {
+    } else if (warp == 4) {
       // inverse of the upper 16 x 16 block, lane c < 16 solving for column
       // c by column-oriented back substitution
       float x[DB];
@@ -991,36 +943,17 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
       if (lane < DB) {
 #pragma unroll
         for (int i4 = 0; i4 < DB; i4 += 4)
-          *(float4*)&Ui[(jb + lane) * TLD + jb + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
+          *(float4*)&UiP[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
       }
     }
     __syncthreads();
-    // column block p of L\U and block row p of L^{-1} are final
+    // column block p of L\U and the two sub-block inverses are final
     {
       const int cs = jb + (t >> 5), r4 = 4 * (t & 31);
       *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
-      const int cl = t >> 2, rl = jb + 4 * (t & 3);
-      *(float4*)(Lo + rl + cl * LU_NB) = *(const float4*)&Li[cl * TLD + rl];
+      SIk[p * 2 * DB * DB + t] = (t < DB * DB) ? LiP[t] : UiP[t - DB * DB];
     }
     // ---- C ----
-    if (t >= 256 && t < 384) {
-      const int r = t - 256;  // Uinv[r, p] = -T_U[r, :] Uinv_pp
-      if (r < jb) {
-        float v[DB], o[DB];
-#pragma unroll
-        for (int q = 0; q < DB; ++q) {
-          v[q] = Ui[(jb + q) * TLD + r];
-          o[q] = 0.f;
-        }
-#pragma unroll
-        for (int c = 0; c < DB; ++c) {
-#pragma unroll
-          for (int q = 0; q <= c; ++q) o[c] = fmaf(-v[q], Ui[(jb + c) * TLD + jb + q], o[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < DB; ++c) Ui[(jb + c) * TLD + r] = o[c];
-      }
-    }
     if (jb + DB < LU_NB) {
       const int n = LU_NB - jb - DB, nt = n / 4;
       const float* Pb = S + jb * TLD + jb + DB;       // L21(r, q)
@@ -1039,11 +972,6 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
       }
     }
     __syncthreads();
-    // block column p of U^{-1} is final
-    {
-      const int cs = jb + (t >> 5), r4 = 4 * (t & 31);
-      *(float4*)(Uo + r4 + cs * LU_NB) = *(const float4*)&Ui[cs * TLD + r4];
-    }
   }
   if (warp == 0) {
     bad = __any_sync(0xffffffffu, bad);
@@ -1052,7 +980,10 @@ __global__ void __launch_bounds__(512, 1) k_diag_factor_tiled(float* __restrict_
 }
 
 constexpr int PW = 32;  // slice width
-constexpr int PANEL_SMEM = sizeof(float) * (LU_NB * TLD + LU_NB * (PW + 4));
+constexpr int PXLD = PW + 4;
+// shared floats of the panel kernel: the factored block, the slice, one
+// side's eight 16 x 16 sub-block inverses
+constexpr int PANEL_SMEM = (int)sizeof(float) * (LU_NB * TLD + LU_NB * PXLD + LU_SI / 2);
 
 __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -1062,80 +993,159 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
 
-// blockIdx.y == 0: U panel, columns [32 x, 32 x + 32) of B (128 rows, ld)
-//   <- Linv B; thread tile rows 4 (t & 31) .. +3, columns 4 (t >> 5) .. +3.
-// blockIdx.y == 1: L panel, rows [32 x, 32 x + 32) of Ap (128 columns, ld)
-//   <- Ap Uinv; thread tile rows 4 (t >> 5) .. +3, columns (t & 31) + 32 j,
-//   written back through shared memory so that the stores coalesce.
-__global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Linv, float* B,
-                                                const float* __restrict__ Uinv, float* Ap, int64_t ld) {
+// Panels of diagonal block k by blocked triangular solves with its factored
+// block Dk (L unit lower and U upper, leading dimension ldk) and its 16 x 16
+// sub-block inverses SIk (from k_diag_lu):
+//   blockIdx.y == 0: columns [32 x, 32 x + 32) of B (128 rows): X = L^{-1} B.
+//     For each sub-block p: X_p = Linv_pp B_p, then B_q -= L_qp X_p (q > p).
+//   blockIdx.y == 1: rows [32 x, 32 x + 32) of Ap (128 columns): X = Ap U^{-1}.
+//     For each sub-block p: X_p = B_p Uinv_pp, then B_q -= X_p U_pq (q > p).
+// ident: the slices start as the corresponding part of the identity (not
+// read), which gives the full inverses L^{-1} and U^{-1} of the block for the
+// triangular sweeps.  B and Ap have leading dimension ld.
+__global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, int64_t ldk,
+                                                const float* __restrict__ SIk, float* B, float* Ap, int64_t ld,
+                                                int ident) {
   extern __shared__ __align__(16) float psm[];
-  float* Ms = psm;                   // Linv or Uinv, column-major, ld TLD
+  float* Ms = psm;                   // factored block, column-major, ld TLD
   float* Xs = psm + LU_NB * TLD;     // the slice
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  if (blockIdx.y == 0) {
+  float* Si = Xs + LU_NB * PXLD;     // [p][16 x 16], column-major
+  const int t = threadIdx.x;
+  const int side = blockIdx.y;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    const int idx = t + 256 * i, r4 = 4 * (idx & 31), kx = idx >> 5;
+    cp_async16(&Ms[kx * TLD + r4], Dk + r4 + (size_t)kx * ldk);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int idx = t + 256 * i, p = idx >> 6, e4 = 4 * (idx & 63);
+    cp_async16(&Si[p * DB * DB + e4], SIk + p * 2 * DB * DB + side * DB * DB + e4);
+  }
+  if (side == 0) {
+    // slice [col][row], ld TLD: Xs[c * TLD + r]
     float* Bb = B + (size_t)blockIdx.x * PW * ld;
+    if (ident) {
+      for (int idx = t; idx < PW * LU_NB; idx += 256) {
+        const int r = idx & (LU_NB - 1), c = idx >> 7;
+        Xs[c * TLD + r] = (r == (int)blockIdx.x * PW + c) ? 1.f : 0.f;
+      }
+    } else {
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int idx = t + 256 * i, r4 = 4 * (idx & 31), kx = idx >> 5;
-      cp_async16(&Ms[kx * TLD + r4], Linv + r4 + kx * LU_NB);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int idx = t + 256 * i, k4 = 4 * (idx & 31), c = idx >> 5;
-      cp_async16(&Xs[c * TLD + k4], Bb + k4 + (size_t)c * ld);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const int r0 = 4 * lane, c0 = 4 * warp;
-    float acc[4][4] = {};
-    tile_mm<4>(Ms, Xs, r0, c0, 0, LU_NB, acc);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      *(float4*)&Bb[r0 + (size_t)(c0 + j) * ld] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
-  } else {
-    float* Ab = Ap + (size_t)blockIdx.x * PW;
-    constexpr int XLD = PW + 4;
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const int idx = t + 256 * i, k4 = 4 * (idx & 31), c = idx >> 5;
-      cp_async16(&Ms[c * TLD + k4], Uinv + k4 + c * LU_NB);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int idx = t + 256 * i, r4 = 4 * (idx & 7), kx = idx >> 3;
-      cp_async16(&Xs[kx * XLD + r4], Ab + r4 + (size_t)kx * ld);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const int r0 = 4 * warp;
-    float acc[4][4] = {};
-    for (int q = 0; q < LU_NB; q += 4) {
-      float4 p[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) p[i] = *(const float4*)&Xs[(q + i) * XLD + r0];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float4 qv = *(const float4*)&Ms[(lane + 32 * j) * TLD + q];
-        const float qq[4] = {qv.x, qv.y, qv.z, qv.w};
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          acc[0][j] = fmaf(p[i].x, qq[i], acc[0][j]);
-          acc[1][j] = fmaf(p[i].y, qq[i], acc[1][j]);
-          acc[2][j] = fmaf(p[i].z, qq[i], acc[2][j]);
-          acc[3][j] = fmaf(p[i].w, qq[i], acc[3][j]);
-        }
+      for (int i = 0; i < 4; ++i) {
+        const int idx = t + 256 * i, k4 = 4 * (idx & 31), c = idx >> 5;
+        cp_async16(&Xs[c * TLD + k4], Bb + k4 + (size_t)c * ld);
       }
     }
+    cp_async_wait_all();
     __syncthreads();
+    for (int p = 0; p < LU_NB / DB; ++p) {
+      const int jb = p * DB;
+      const float* Li = Si + p * DB * DB;  // Linv_pp(i, q) = Li[q * 16 + i]
+      {
+        // X_p = Linv_pp B_p: thread -> column t / 8, rows 2 (t % 8) .. +1
+        const int c = t >> 3, r2 = 2 * (t & 7);
+        float o0 = 0.f, o1 = 0.f;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-      *(float4*)&Xs[(lane + 32 * j) * XLD + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+        for (int q = 0; q < DB; ++q) {
+          const float b = Xs[c * TLD + jb + q];
+          o0 = fmaf(Li[q * DB + r2], b, o0);
+          o1 = fmaf(Li[q * DB + r2 + 1], b, o1);
+        }
+        __syncthreads();
+        Xs[c * TLD + jb + r2] = o0;
+        Xs[c * TLD + jb + r2 + 1] = o1;
+      }
+      __syncthreads();
+      // B_q -= L_qp X_p: thread -> row jb + 16 + (t % 128), 16 columns
+      const int i = jb + DB + (t & (LU_NB - 1));
+      if (i < LU_NB) {
+        float l[DB];
+#pragma unroll
+        for (int q = 0; q < DB; ++q) l[q] = Ms[(jb + q) * TLD + i];
+        const int cb = (t >> 7) * (PW / 2);
+#pragma unroll 4
+        for (int cc = 0; cc < PW / 2; ++cc) {
+          const int c = cb + cc;
+          const float* xp = Xs + c * TLD + jb;
+          float acc = Xs[c * TLD + i];
+#pragma unroll
+          for (int q4 = 0; q4 < DB; q4 += 4) {
+            const float4 x = *(const float4*)&xp[q4];
+            acc = fmaf(-l[q4], x.x, acc);
+            acc = fmaf(-l[q4 + 1], x.y, acc);
+            acc = fmaf(-l[q4 + 2], x.z, acc);
+            acc = fmaf(-l[q4 + 3], x.w, acc);
+          }
+          Xs[c * TLD + i] = acc;
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = t + 256 * i, r4 = 4 * (idx & 31), c = idx >> 5;
+      *(float4*)&Bb[r4 + (size_t)c * ld] = *(const float4*)&Xs[c * TLD + r4];
+    }
+  } else {
+    // slice [col][row], ld PXLD: Xs[c * PXLD + r], 32 rows
+    float* Ab = Ap + (size_t)blockIdx.x * PW;
+    if (ident) {
+      for (int idx = t; idx < PW * LU_NB; idx += 256) {
+        const int r = idx & (PW - 1), c = idx >> 5;
+        Xs[c * PXLD + r] = ((int)blockIdx.x * PW + r == c) ? 1.f : 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int idx = t + 256 * i, r4 = 4 * (idx & 7), kx = idx >> 3;
+        cp_async16(&Xs[kx * PXLD + r4], Ab + r4 + (size_t)kx * ld);
+      }
+    }
+    cp_async_wait_all();
     __syncthreads();
+    const int r = t & (PW - 1), g = t >> 5;
+    for (int p = 0; p < LU_NB / DB; ++p) {
+      const int jb = p * DB;
+      const float* Ui = Si + p * DB * DB;  // Uinv_pp(q, c) = Ui[c * 16 + q]
+      {
+        // X_p = B_p Uinv_pp: thread -> row t % 32, columns 2 (t / 32) .. +1
+        const int c2 = 2 * g;
+        float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < DB; ++q) {
+          const float b = Xs[(jb + q) * PXLD + r];
+          o0 = fmaf(b, Ui[c2 * DB + q], o0);
+          o1 = fmaf(b, Ui[(c2 + 1) * DB + q], o1);
+        }
+        __syncthreads();
+        Xs[(jb + c2) * PXLD + r] = o0;
+        Xs[(jb + c2 + 1) * PXLD + r] = o1;
+      }
+      __syncthreads();
+      // B_q -= X_p U_pq: thread -> row t % 32, columns jb + 16 + t / 32 + 8 m
+      float x[DB];
+#pragma unroll
+      for (int q = 0; q < DB; ++q) x[q] = Xs[(jb + q) * PXLD + r];
+      for (int c = jb + DB + g; c < LU_NB; c += 8) {
+        const float* up = Ms + c * TLD + jb;
+        float acc = Xs[c * PXLD + r];
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4) {
+          const float4 u = *(const float4*)&up[q4];
+          acc = fmaf(-x[q4], u.x, acc);
+          acc = fmaf(-x[q4 + 1], u.y, acc);
+          acc = fmaf(-x[q4 + 2], u.z, acc);
+          acc = fmaf(-x[q4 + 3], u.w, acc);
+        }
+        Xs[c * PXLD + r] = acc;
+      }
+      __syncthreads();
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = t + 256 * i, r4 = 4 * (idx & 7), c = idx >> 3;
-      *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&Xs[c * XLD + r4];
+      *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&Xs[c * PXLD + r4];
     }
   }
 }
@@ -1232,7 +1242,7 @@ static void lu_attrs() {
 static void lu_attrs_once() {
   cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float) * LU_NB * DLD));
-  cudaFuncSetAttribute(k_diag_factor_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
+  cudaFuncSetAttribute(k_diag_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
   cudaFuncSetAttribute(k_gemm_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
   cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1241,33 +1251,48 @@ static void lu_attrs_once() {
   cudaFuncSetAttribute(k_thin_update, cudaFuncAttributeMaxDynamicSharedMemorySize, THIN_SMEM);
 }
 
+// sub-block inverses of diagonal block k (after the full inverses in Dinv)
+static float* sub_inverses(float* Dinv, int Npad, int k) {
+  return Dinv + (size_t)(Npad / LU_NB) * 2 * LU_NB * LU_NB + (size_t)k * LU_SI;
+}
+
 // diagonal block k
-static void diag_block(float* A, int64_t ld, float* Dinv, int* info, int k, cudaStream_t st) {
+static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st) {
   KScope kd(st, KC_LU_DIAG);
-  k_diag_factor_tiled<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, Dinv, info);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info);
   count_launches(1);
 }
 
-// the two panels of diagonal block k: U12 = Linv A12, L21 = A21 Uinv
+// the two panels of diagonal block k: U12 = L^{-1} A12, L21 = A21 U^{-1}
 static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st) {
   const size_t kk = (size_t)k * LU_NB;
   const int rem = Npad - (int)kk - LU_NB;
   if (rem <= 0) return;
-  const float* Li = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
-  const float* Ui = Li + LU_NB * LU_NB;
   float* A12 = A + kk + (kk + LU_NB) * ld;
   float* A21 = A + (kk + LU_NB) + kk * ld;
   KScope kp(st, KC_LU_PANELS);
-  k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(Li, A12, Ui, A21, ld);
+  k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k), A12,
+                                                       A21, ld, 0);
   count_launches(1);
 }
 
-// diagonal block k and its two panels (panels in full FP32 on the CUDA cores)
+// the full inverses of the unit-lower and upper triangles of diagonal block
+// k into Dinv (for the triangular sweeps; off the factorization's chain)
+static void block_inverses(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st) {
+  const size_t kk = (size_t)k * LU_NB;
+  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
+  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k), Lo,
+                                                         Lo + LU_NB * LU_NB, LU_NB, 1);
+  count_launches(1);
+}
+
+// diagonal block k, its panels and its inverses on one stream
 static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, int k,
                             cudaStream_t st) {
   (void)x3;
-  diag_block(A, ld, Dinv, info, k, st);
+  diag_block(A, ld, Npad, Dinv, info, k, st);
   panels(A, ld, Npad, Dinv, k, st);
+  block_inverses(A, ld, Npad, Dinv, k, st);
 }
 
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
@@ -1294,23 +1319,28 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
   return (int)cudaGetLastError();
 }
 
-// Lookahead-1 schedule on two streams.  `la` (the critical path) finishes
-// the thin part of step k's update -- block column k+1 and block row k+1,
-// one FP32 launch -- then factors diagonal block k+1 and its panels; `st`
-// splits step k's panels into the tensor-core operands and runs the bulk of
-// step k's trailing update meanwhile.  evP[k]: panels of step k ready;
-// evT[k]: bulk update of step k done.  tc[2]: plans with separate
-// lo/transposed buffers for even and odd steps.
+// Lookahead-1 schedule on three streams.  `la` (the critical path)
+// finishes the thin part of step k's update -- block column k+1 and block
+// row k+1, one FP32 launch -- then factors diagonal block k+1 and its
+// panels; `st` splits step k's panels into the tensor-core operands and runs
+// the bulk of step k's trailing update meanwhile; `iv` forms the full
+// inverses of each diagonal block once its panels are done.  evP[k]: panels
+// of step k ready; evT[k]: bulk update of step k done; ivdone: all inverses
+// formed.  tc[2]: plans with separate lo/transposed buffers for even and odd
+// steps.
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        const TcPlan* tc, int* err) {
+                        cudaStream_t iv, cudaEvent_t ivdone, const TcPlan* tc, int* err) {
   const int K = Npad / LU_NB;
   lu_attrs();
   KScope total(st, KC_LU_TOTAL);
   cudaEventRecord(fork, st);
   cudaStreamWaitEvent(la, fork, 0);
-  diag_and_panels(A, ld, Npad, Dinv, info, 1, 0, la);
+  diag_block(A, ld, Npad, Dinv, info, 0, la);
+  panels(A, ld, Npad, Dinv, 0, la);
   cudaEventRecord(evP[0], la);
+  cudaStreamWaitEvent(iv, evP[0], 0);
+  block_inverses(A, ld, Npad, Dinv, 0, iv);
   for (int k = 0; k + 1 < K; ++k) {
     const int rem = Npad - (k + 1) * LU_NB;
     const TcPlan& P = tc[k & 1];
@@ -1318,9 +1348,12 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     {
       KScope crit(la, KC_LU_CRIT);
       thin_update(A, ld, k, rem, la);  // block column and block row k+1
-      diag_and_panels(A, ld, Npad, Dinv, info, 1, k + 1, la);
+      diag_block(A, ld, Npad, Dinv, info, k + 1, la);
+      panels(A, ld, Npad, Dinv, k + 1, la);
     }
     cudaEventRecord(evP[k + 1], la);
+    cudaStreamWaitEvent(iv, evP[k + 1], 0);
+    block_inverses(A, ld, Npad, Dinv, k + 1, iv);
     cudaStreamWaitEvent(st, evP[k], 0);
     if (rem > LU_NB) {
       KScope trail(st, KC_LU_TRAIL);
@@ -1331,6 +1364,8 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     cudaEventRecord(evT[k], st);
   }
   cudaStreamWaitEvent(st, evP[K - 1], 0);
+  cudaEventRecord(ivdone, iv);
+  cudaStreamWaitEvent(st, ivdone, 0);
   return (int)cudaGetLastError();
 }
 
@@ -1467,10 +1502,12 @@ namespace bem {
 // Self-check: factor the diagonal block at (0, 0) of A1 with the blocked
 // kernel and of A2 (a copy) with the register-blocked Gauss-Jordan kernel;
 // D1, D2 receive the two pairs of triangular inverses.
-void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, int* info, cudaStream_t st) {
+void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float* SI, int* info,
+                   cudaStream_t st) {
   lu_attrs();
-  k_diag_factor_tiled<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, D1, info);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info);
+  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
-  count_launches(2);
+  count_launches(3);
 }
 }  // namespace bem

@@ -111,7 +111,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   cudaStream_t st = c->stream;
   float* A32 = (float*)c->get(bem_ctx::SLOT_LU0, sizeof(float) * (size_t)Npad * Npad);
   double* cs = (double*)c->get(bem_ctx::SLOT_LU1, sizeof(double) * (size_t)N);
-  float* Dinv = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * (size_t)K * 2 * LU_NB * LU_NB);
+  float* Dinv = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * bem::lu_dinv_floats(K));
   double* V = (double*)c->get(bem_ctx::SLOT_LU3, sizeof(double) * (size_t)N * (m + 1));
   double* Z = (double*)c->get(bem_ctx::SLOT_LU4, sizeof(double) * (size_t)N * m);
   double* w = (double*)c->get(bem_ctx::SLOT_LU5, sizeof(double) * ((size_t)N + 64));
@@ -147,7 +147,8 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   int rc;
   if (use_tc && tcp[0].ok && tcp[1].ok)
     rc = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
-                                  c->events.data(), c->events.data() + K, tcp, werr);
+                                  c->events.data(), c->events.data() + K,
+                                  c->inv_stream, c->inv_done, tcp, werr);
   else
     rc = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
   if (rc) return c->cuda_fail((cudaError_t)rc, "lu_factor");
@@ -517,13 +518,13 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   if (which == 2) {
     float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
     float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);
-    float* D = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * 4 * LU_NB * LU_NB);
+    float* D = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * (4 * LU_NB * LU_NB + LU_SI));
     int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
     if (!A1 || !A2 || !D || !info) return BEM_ERR_NOMEM;
     k_fill_test<<<1024, 256, 0, st>>>(A1, n, n, 777u);
     cudaMemcpyAsync(A2, A1, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(info, 0, 16, st);
-    bem::diag_selftest(A1, A2, n, D, D + 2 * LU_NB * LU_NB, info, st);
+    bem::diag_selftest(A1, A2, n, D, D + 2 * LU_NB * LU_NB, D + 4 * LU_NB * LU_NB, info, st);
     float* d = (float*)(info + 8);
     float h[6];
     cudaMemsetAsync(d, 0, 24, st);
@@ -538,7 +539,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   const int K = n / LU_NB;
   float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
   float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);
-  float* Dinv = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * (size_t)K * 2 * LU_NB * LU_NB);
+  float* Dinv = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * bem::lu_dinv_floats(K));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
   float* Lt = (float*)c->get(bem_ctx::SLOT_TC0, sizeof(float) * (size_t)n * LU_NB);
   float* Ltlo = (float*)c->get(bem_ctx::SLOT_TC1, sizeof(float) * (size_t)n * LU_NB);
@@ -559,7 +560,8 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   Timer t1, t2;
   t1.start(st);
   int rc = bem::lu_factor_lookahead(A1, n, n, Dinv, info, st, c->la_stream, c->fork_event,
-                                    c->events.data(), c->events.data() + K, tcp, info + 1);
+                                    c->events.data(), c->events.data() + K,
+                                  c->inv_stream, c->inv_done, tcp, info + 1);
   t1.stop(st);
   if (rc) return c->cuda_fail((cudaError_t)rc, "selftest tcgen05 LU");
   t2.start(st);
