@@ -43,10 +43,11 @@ struct bem_ctx {
   cudaStream_t la_stream = nullptr;
   cudaEvent_t fork_event = nullptr;
   std::vector<cudaEvent_t> events;
-  // third stream of the lookahead LU (diagonal-block inverses) and its end
-  cudaStream_t inv_stream = nullptr;
+  // third and fourth streams of the lookahead LU (diagonal-block inverses,
+  // thin updates)
+  cudaStream_t inv_stream = nullptr, thin_stream = nullptr;
   cudaEvent_t inv_done = nullptr;
-  // Ensures 2*k events and the lookahead stream; false on failure.
+  // Ensures 3*k events and the lookahead streams; false on failure.
   bool lookahead_ready(int k);
 
   // Grow-only device buffer for `slot` (NULL on allocation failure).

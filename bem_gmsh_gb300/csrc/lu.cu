@@ -748,15 +748,22 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 //      16 x 16 block.  Column block p of L\U and both sub-block inverses are
 //      final and are written out.
 //   C  the trailing update A22 -= L21 U12 on 4 x 4 register tiles.
-// 24 block barriers in all; 70 KB of shared memory, so the kernel starts
-// beside a bulk-update tile.  A and ld must allow 16-byte accesses (ld % 4 ==
-// 0, 16-byte aligned A).
+// 24 block barriers in all.  With `pre` the block first gets the update of
+// the previous step, A_kk -= L_{k,k-1} U_{k-1,k} (K = 128 in chunks of 32),
+// which the look-ahead otherwise leaves to the thin update, so that the rest
+// of that update runs beside this kernel.  105 KB of shared memory, so the
+// kernel starts beside a bulk-update tile.  A and ld must allow 16-byte
+// accesses (ld % 4 == 0, 16-byte aligned A).
 // ---------------------------------------------------------------------------
 constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
 // shared floats of the diagonal kernel: L\U, four double-buffered pivot
-// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses
-constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 2 * DB * DB);
+// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses,
+// the operand chunks of the pre-update (L 128 x 32, U 32 x 128)
+constexpr int PRE_KC = 32;
+constexpr int PRE_ULD = PRE_KC + 4;
+constexpr int DIAG_SMEM =
+    (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 2 * DB * DB + PRE_KC * TLD + LU_NB * PRE_ULD);
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -798,13 +805,15 @@ __device__ __forceinline__ float rcp_nr(float x) {
 }
 
 __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64_t ld, int k,
-                                                 float* __restrict__ SI, int* __restrict__ info) {
+                                                 float* __restrict__ SI, int* __restrict__ info, int pre) {
   extern __shared__ __align__(16) float dsm[];
   float* S = dsm;                       // A -> L\U
   float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
   float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
   float* LiP = Ls + 16 * 20;            // Linv_pp, column-major, ld 16
   float* UiP = LiP + DB * DB;           // Uinv_pp, column-major, ld 16
+  float* Lc = UiP + DB * DB;            // pre-update L chunk [q][r], ld TLD
+  float* Uc = Lc + PRE_KC * TLD;        // pre-update U chunk [c][q], ld PRE_ULD
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
   float* Ab = A + off + off * ld;
@@ -821,6 +830,43 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
     for (int i = 0; i < 8; ++i) {
       const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
       *(float4*)&S[c * TLD + r4] = v[i];
+    }
+  }
+  if (pre && k > 0) {
+    // A_kk -= L_{k,k-1} U_{k-1,k}: thread -> rows 4 (t % 32) .. +3,
+    // columns 8 (t / 32) .. +7
+    const float* Lb = Ab - LU_NB * ld;  // block (k, k-1)
+    const float* Ub = Ab - LU_NB;       // block (k-1, k)
+    const int r0 = 4 * (t & 31), c0 = 8 * (t >> 5);
+    float acc[4][8] = {};
+    for (int kc = 0; kc < LU_NB; kc += PRE_KC) {
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int idx = t + 512 * i, r4 = 4 * (idx & 31), q = idx >> 5;  // 32 columns of L
+        *(float4*)&Lc[q * TLD + r4] = __ldcg((const float4*)(Lb + r4 + (size_t)(kc + q) * ld));
+        const int q4 = 4 * (idx & 7), c = idx >> 3;                    // 128 columns of U
+        *(float4*)&Uc[c * PRE_ULD + q4] = __ldcg((const float4*)(Ub + kc + q4 + (size_t)c * ld));
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int q = 0; q < PRE_KC; ++q) {
+        const float4 a = *(const float4*)&Lc[q * TLD + r0];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float b = Uc[(c0 + j) * PRE_ULD + q];
+          acc[0][j] = fmaf(a.x, b, acc[0][j]);
+          acc[1][j] = fmaf(a.y, b, acc[1][j]);
+          acc[2][j] = fmaf(a.z, b, acc[2][j]);
+          acc[3][j] = fmaf(a.w, b, acc[3][j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float4 v = *(float4*)&S[(c0 + j) * TLD + r0];
+      v.x -= acc[0][j]; v.y -= acc[1][j]; v.z -= acc[2][j]; v.w -= acc[3][j];
+      *(float4*)&S[(c0 + j) * TLD + r0] = v;
     }
   }
   __syncthreads();
@@ -1230,9 +1276,6 @@ static void thin_part(float* A, int64_t ld, int k, int rem, int ro, int M0, bool
   k_thin_update<<<tiles, 256, THIN_SMEM, st>>>(A, ld, k * LU_NB, rem, ro, M0);
   count_launches(1);
 }
-static void thin_update(float* A, int64_t ld, int k, int rem, cudaStream_t st) {
-  thin_part(A, ld, k, rem, 0, rem, true, st);
-}
 
 static void lu_attrs_once();
 static void lu_attrs() {
@@ -1257,9 +1300,11 @@ static float* sub_inverses(float* Dinv, int Npad, int k) {
 }
 
 // diagonal block k
-static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st) {
+// (pre: with the update by panel k-1 of its own block, see k_diag_lu)
+static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st,
+                       int pre = 0) {
   KScope kd(st, KC_LU_DIAG);
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info, pre);
   count_launches(1);
 }
 
@@ -1319,18 +1364,20 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
   return (int)cudaGetLastError();
 }
 
-// Lookahead-1 schedule on three streams.  `la` (the critical path)
-// finishes the thin part of step k's update -- block column k+1 and block
-// row k+1, one FP32 launch -- then factors diagonal block k+1 and its
-// panels; `st` splits step k's panels into the tensor-core operands and runs
-// the bulk of step k's trailing update meanwhile; `iv` forms the full
-// inverses of each diagonal block once its panels are done.  evP[k]: panels
-// of step k ready; evT[k]: bulk update of step k done; ivdone: all inverses
-// formed.  tc[2]: plans with separate lo/transposed buffers for even and odd
-// steps.
+// Lookahead-1 schedule on four streams.  `la` (the critical path) factors
+// diagonal block k+1, applying step k's update to that block itself, then
+// its panels; `tl` meanwhile applies the rest of step k's thin update (block
+// column k+1 below the diagonal block and block row k+1 right of it, FP32);
+// `st` splits step k's panels into the tensor-core operands and runs the
+// bulk of step k's trailing update; `iv` forms the full inverses of each
+// diagonal block once its panels are done.  evP[k]: panels of step k ready;
+// evT[k]: bulk update of step k done; evR[k]: thin update of step k done;
+// ivdone: all inverses formed.  tc[2]: plans with separate lo/transposed
+// buffers for even and odd steps.
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        cudaStream_t iv, cudaEvent_t ivdone, const TcPlan* tc, int* err) {
+                        cudaStream_t tl, cudaEvent_t* evR, cudaStream_t iv, cudaEvent_t ivdone,
+                        const TcPlan* tc, int* err) {
   const int K = Npad / LU_NB;
   lu_attrs();
   KScope total(st, KC_LU_TOTAL);
@@ -1345,10 +1392,16 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     const int rem = Npad - (k + 1) * LU_NB;
     const TcPlan& P = tc[k & 1];
     if (k >= 1) cudaStreamWaitEvent(la, evT[k - 1], 0);
+    // thin update of step k without the diagonal block: needs panels k
+    // (evP[k]) and the bulk update of step k-1
+    cudaStreamWaitEvent(tl, evP[k], 0);
+    if (k >= 1) cudaStreamWaitEvent(tl, evT[k - 1], 0);
+    thin_part(A, ld, k, rem, LU_NB, rem - LU_NB, true, tl);
+    cudaEventRecord(evR[k], tl);
     {
       KScope crit(la, KC_LU_CRIT);
-      thin_update(A, ld, k, rem, la);  // block column and block row k+1
-      diag_block(A, ld, Npad, Dinv, info, k + 1, la);
+      diag_block(A, ld, Npad, Dinv, info, k + 1, la, 1);
+      cudaStreamWaitEvent(la, evR[k], 0);
       panels(A, ld, Npad, Dinv, k + 1, la);
     }
     cudaEventRecord(evP[k + 1], la);
@@ -1505,7 +1558,7 @@ namespace bem {
 void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float* SI, int* info,
                    cudaStream_t st) {
   lu_attrs();
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info, 0);
   k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
   count_launches(3);

@@ -148,7 +148,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   if (use_tc && tcp[0].ok && tcp[1].ok)
     rc = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
                                   c->events.data(), c->events.data() + K,
-                                  c->inv_stream, c->inv_done, tcp, werr);
+                                  c->thin_stream, c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, werr);
   else
     rc = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
   if (rc) return c->cuda_fail((cudaError_t)rc, "lu_factor");
@@ -561,7 +561,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   t1.start(st);
   int rc = bem::lu_factor_lookahead(A1, n, n, Dinv, info, st, c->la_stream, c->fork_event,
                                     c->events.data(), c->events.data() + K,
-                                  c->inv_stream, c->inv_done, tcp, info + 1);
+                                  c->thin_stream, c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, info + 1);
   t1.stop(st);
   if (rc) return c->cuda_fail((cudaError_t)rc, "selftest tcgen05 LU");
   t2.start(st);
