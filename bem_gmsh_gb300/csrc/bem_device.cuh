@@ -646,13 +646,16 @@ __device__ inline void integrate_singular(const Rules& R, const Physics& ph, con
       }
     }
   }
-  // G: log coefficient by least squares (_interp_log_coeff)
+  // G: log coefficient by least squares (_interp_log_coeff); log |d_i| is
+  // formed once per sample (FP64 logs dominate this routine)
+  double lgd[BEM_NINTERP];
   double sL = 0.0, sL2 = 0.0;
   int nused = 0;
   for (int i = 0; i < m; ++i) {
     double adi = fabs(d[i]);
+    lgd[i] = log(adi);
     if (adi < 1e-14) continue;
-    double lg = log(adi);
+    double lg = lgd[i];
     sL += lg;
     sL2 += lg * lg;
     ++nused;
@@ -667,14 +670,14 @@ __device__ inline void integrate_singular(const Rules& R, const Physics& ph, con
     for (int i = 0; i < m; ++i) {
       double adi = fabs(d[i]);
       if (adi < 1e-14) continue;
-      double lg = log(adi);
+      double lg = lgd[i];
       double wi = Fg[i * K + c] - Fm1 / d[i];
       sW += wi;
       sWL += wi * lg;
     }
     double F0 = fit ? (nused * sWL - sL * sW) / detA : 0.0;
-    double acc = wq[0] * (Fg[c] - Fm1 / d[0] - F0 * log(fabs(d[0])));
-    for (int i = 1; i < m; ++i) acc += wq[i] * (Fg[i * K + c] - Fm1 / d[i] - F0 * log(fabs(d[i])));
+    double acc = wq[0] * (Fg[c] - Fm1 / d[0] - F0 * lgd[0]);
+    for (int i = 1; i < m; ++i) acc += wq[i] * (Fg[i * K + c] - Fm1 / d[i] - F0 * lgd[i]);
     g[c] = acc + (Fm1 * hp1 + F0 * lp);
   }
   // H: CPV cascade (_interp_cascade, order -1)
