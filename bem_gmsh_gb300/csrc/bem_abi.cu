@@ -108,6 +108,16 @@ void build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules& R) 
     R.gi_bw[i] = 1.0 / b;
   }
   for (int k = 0; k < nn; ++k) R.ew[k] = ew_host[k];
+  auto product_weights = [](const double* xs, int n, double* pw) {
+    for (int i = 0; i < n; ++i) {
+      long double b = 1.0L;
+      for (int j = 0; j < n; ++j)
+        if (j != i) b *= (long double)xs[i] - (long double)xs[j];
+      pw[i] = (double)(1.0L / b);
+    }
+  };
+  product_weights(R.leg_x, nn, R.leg_pw);
+  if (g->ngeo > 0) product_weights(R.geo_x, g->ngeo, R.geo_pw);
 }
 
 }  // namespace

@@ -36,6 +36,9 @@ struct Rules {
   double qsi[BEM_MAXNPG], w[BEM_MAXNPG];
   double gi_x[BEM_NINTERP], gi_w[BEM_NINTERP], gi_bw[BEM_NINTERP];
   double ew[BEM_MAXNN];  // element Gauss weights (elem_weight)
+  // product-form weights 1 / prod_{j != i} (x_i - x_j) of the field and CAD
+  // nodes (the barycentric weights above carry an arbitrary scale)
+  double leg_pw[BEM_MAXNN], geo_pw[BEM_MAXGEO];
 };
 
 // Physics of one assembly.
@@ -79,6 +82,34 @@ __device__ __forceinline__ void shapefun(const double* nodes, const double* bw, 
     L[exact] = 1.0;
   } else {
     for (int i = 0; i < n; ++i) L[i] /= msum;
+  }
+  if (dL) {
+    for (int j = 0; j < n; ++j) {
+      double s = L[0] * D[j];
+      for (int i = 1; i < n; ++i) s += L[i] * D[i * n + j];
+      dL[j] = s;
+    }
+  }
+}
+
+// The same basis in product form, L_i(x) = w_i prod_{j != i} (x - x_j) with
+// the product-form weights w_i = 1 / prod_{j != i} (x_i - x_j): no division
+// (GB300 runs FP64 division as a long sequence on its small FP64 pipe); it
+// differs from the barycentric form by rounding only (n <= 6 nodes on
+// [-1, 1]).  Used per quadrature point of the element integrals.
+__device__ __forceinline__ void shapefun_prod(const double* nodes, const double* bw, const double* D, int n,
+                                              double xx, double* L, double* dL) {
+  double d[BEM_MAXGEO > BEM_MAXNN ? BEM_MAXGEO : BEM_MAXNN];
+  for (int i = 0; i < n; ++i) d[i] = xx - nodes[i];
+  double pre = 1.0;
+  for (int i = 0; i < n; ++i) {
+    L[i] = bw[i] * pre;
+    pre *= d[i];
+  }
+  double suf = 1.0;
+  for (int i = n - 1; i >= 0; --i) {
+    L[i] *= suf;
+    suf *= d[i];
   }
   if (dL) {
     for (int j = 0; j < n; ++j) {
@@ -505,10 +536,11 @@ __device__ inline int tanp3ctrans(const Rules& R, double z0, double e0, double* 
 __device__ __forceinline__ void shape_geom(const Rules& R, const V2* nodes, const V2* geo, double xi,
                                            double* N, V2& pg, V2& dx) {
   double dN[BEM_MAXNN];
-  shapefun(R.leg_x, R.leg_bw, R.leg_D, R.nn, xi, N, dN);
   if (R.ngeo > 0) {
+    // field basis without derivatives: the geometry comes from the CAD nodes
+    shapefun_prod(R.leg_x, R.leg_pw, R.leg_D, R.nn, xi, N, nullptr);
     double Ng[BEM_MAXGEO], dNg[BEM_MAXGEO];
-    shapefun(R.geo_x, R.geo_bw, R.geo_D, R.ngeo, xi, Ng, dNg);
+    shapefun_prod(R.geo_x, R.geo_pw, R.geo_D, R.ngeo, xi, Ng, dNg);
     pg = V2{0.0, 0.0};
     dx = V2{0.0, 0.0};
     for (int k = 0; k < R.ngeo; ++k) {
@@ -519,6 +551,7 @@ __device__ __forceinline__ void shape_geom(const Rules& R, const V2* nodes, cons
     }
     return;
   }
+  shapefun_prod(R.leg_x, R.leg_pw, R.leg_D, R.nn, xi, N, dN);
   pg = V2{0.0, 0.0};
   dx = V2{0.0, 0.0};
   for (int k = 0; k < R.nn; ++k) {
@@ -552,7 +585,8 @@ __device__ inline void integrate_near(const Rules& R, const Physics& ph, const V
     shape_geom(R, nodes, geo, eta[i], N, pg, dx);
     double rx = pg.x - pf.x, ry = pg.y - pf.y;
     double J = vnorm(dx.x, dx.y);
-    double tx = dx.x / J, ty = dx.y / J;
+    const double invJ = 1.0 / J;
+    double tx = dx.x * invJ, ty = dx.y * invJ;
     double nxq = ty, nyq = -tx;
     if (i == 0 && (nxq * nref.x + nyq * nref.y) < 0) flip = -1.0;
     nxq *= flip;
@@ -623,6 +657,8 @@ __device__ inline void integrate_singular(const Rules& R, const Physics& ph, con
     }
     for (int i = 0; i < m; ++i) d[i] = xi[i] - a;
   }
+  double invd[BEM_NINTERP];
+  for (int i = 0; i < m; ++i) invd[i] = 1.0 / d[i];
   // samples
   double Fg[BEM_NINTERP * BEM_MAXNN * NC], Fh[BEM_NINTERP * BEM_MAXNN * NC];
   for (int i = 0; i < m; ++i) {
@@ -634,7 +670,8 @@ __device__ inline void integrate_singular(const Rules& R, const Physics& ph, con
     bool ok = !(J < 1e-30) && !(vnorm(rx, ry) < 1e-30);
     double U[4] = {0, 0, 0, 0}, T[4] = {0, 0, 0, 0};
     if (ok) {
-      double nxq = dx.y / J, nyq = -(dx.x / J);
+      const double invJ = 1.0 / J;
+      double nxq = dx.y * invJ, nyq = -(dx.x * invJ);
       if (nxq * nref.x + nyq * nref.y < 0) { nxq = -nxq; nyq = -nyq; }
       eval_kernel<NC>(ph, rx, ry, nxq, nyq, U, T);
     }
@@ -671,21 +708,21 @@ __device__ inline void integrate_singular(const Rules& R, const Physics& ph, con
       double adi = fabs(d[i]);
       if (adi < 1e-14) continue;
       double lg = lgd[i];
-      double wi = Fg[i * K + c] - Fm1 / d[i];
+      double wi = Fg[i * K + c] - Fm1 * invd[i];
       sW += wi;
       sWL += wi * lg;
     }
     double F0 = fit ? (nused * sWL - sL * sW) / detA : 0.0;
-    double acc = wq[0] * (Fg[c] - Fm1 / d[0] - F0 * lgd[0]);
-    for (int i = 1; i < m; ++i) acc += wq[i] * (Fg[i * K + c] - Fm1 / d[i] - F0 * lgd[i]);
+    double acc = wq[0] * (Fg[c] - Fm1 * invd[0] - F0 * lgd[0]);
+    for (int i = 1; i < m; ++i) acc += wq[i] * (Fg[i * K + c] - Fm1 * invd[i] - F0 * lgd[i]);
     g[c] = acc + (Fm1 * hp1 + F0 * lp);
   }
   // H: CPV cascade (_interp_cascade, order -1)
   for (int c = 0; c < K; ++c) {
     double F1 = Ni[0] * (Fh[c] * d[0]);
     for (int i = 1; i < m; ++i) F1 += Ni[i] * (Fh[i * K + c] * d[i]);
-    double acc = wq[0] * (Fh[c] - F1 / d[0]);
-    for (int i = 1; i < m; ++i) acc += wq[i] * (Fh[i * K + c] - F1 / d[i]);
+    double acc = wq[0] * (Fh[c] - F1 * invd[0]);
+    for (int i = 1; i < m; ++i) acc += wq[i] * (Fh[i * K + c] - F1 * invd[i]);
     h[c] = acc + F1 * hp1;
   }
 }
