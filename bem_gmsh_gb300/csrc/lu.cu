@@ -751,9 +751,11 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 // 24 block barriers in all.  With `pre` the block first gets the update of
 // the previous step, A_kk -= L_{k,k-1} U_{k-1,k} (K = 128 in chunks of 32),
 // which the look-ahead otherwise leaves to the thin update, so that the rest
-// of that update runs beside this kernel.  105 KB of shared memory, so the
-// kernel starts beside a bulk-update tile.  A and ld must allow 16-byte
-// accesses (ld % 4 == 0, 16-byte aligned A).
+// of that update runs beside this kernel.  105 KB of shared memory and the
+// whole register file (512 threads x 128): the kernel runs alone on an SM
+// (capped at 64 registers to share an SM with a bulk-update tile it measured
+// 40 % slower).  A and ld must allow 16-byte accesses (ld % 4 == 0, 16-byte
+// aligned A).
 // ---------------------------------------------------------------------------
 constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
