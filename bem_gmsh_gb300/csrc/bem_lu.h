@@ -41,6 +41,8 @@ void dots64(const double* V, int64_t ldv, int N, int m, const double* w, double*
 void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, double* w, cudaStream_t st);
 void add_zy64(const double* Z, int64_t ldz, int N, int m, const double* y, double* x, cudaStream_t st);
 void scale_copy64(const double* w, double s, double* v, int N, cudaStream_t st);
+// v = w / sqrt(*n2), n2 on the device
+void scale_by_norm64(const double* w, const double* n2, double* v, int N, cudaStream_t st);
 void to_f32(const double* v, int N, int Npad, float* o, cudaStream_t st);
 void from_f32_scale(const float* y, const double* cs, int N, double* z, cudaStream_t st);
 

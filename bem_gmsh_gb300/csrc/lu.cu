@@ -705,6 +705,15 @@ __global__ void k_add_zy(const double* __restrict__ Z, int64_t ldz, int N, int m
   }
 }
 
+// v = w / sqrt(*n2) (zeros when *n2 is not positive): normalization by a
+// norm that stays on the device
+__global__ void k_scale_by_norm(const double* __restrict__ w, const double* __restrict__ n2,
+                                double* __restrict__ v, int N) {
+  const double q = *n2;
+  const double s = q > 0.0 ? 1.0 / sqrt(q) : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) v[i] = w[i] * s;
+}
+
 __global__ void k_scale_copy(const double* __restrict__ w, double s, double* __restrict__ v, int N) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) v[i] = w[i] * s;
 }
@@ -1537,6 +1546,10 @@ void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, doubl
 void add_zy64(const double* Z, int64_t ldz, int N, int m, const double* y, double* x, cudaStream_t st) {
   count_launches(1);
   k_add_zy<<<(N + 255) / 256, 256, 0, st>>>(Z, ldz, N, m, y, x);
+}
+void scale_by_norm64(const double* w, const double* n2, double* v, int N, cudaStream_t st) {
+  count_launches(1);
+  k_scale_by_norm<<<(N + 255) / 256, 256, 0, st>>>(w, n2, v, N);
 }
 void scale_copy64(const double* w, double s, double* v, int N, cudaStream_t st) {
   count_launches(1);

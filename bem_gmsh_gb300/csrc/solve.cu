@@ -209,18 +209,22 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       double* zj = Z + (size_t)j * N;
       precond(V + (size_t)j * N, zj);
       bem::gemv64(A64, lda, N, zj, w, st);
-      // classical Gram-Schmidt, two passes
-      std::vector<double> h(j + 2, 0.0), h2(j + 1);
+      // classical Gram-Schmidt, two passes, and the normalization, all on
+      // the device (pass p's coefficients in hbuf[32 p ..], the squared
+      // norm in hbuf[62]); one copy brings them to the host
       for (int pass = 0; pass < 2; ++pass) {
-        bem::dots64(V, N, N, j + 1, w, hbuf, st);
-        bem::sub_vh64(V, N, N, j + 1, hbuf, w, st);
-        cudaMemcpyAsync(h2.data(), hbuf, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, st);
-        cudaStreamSynchronize(st);
-        for (int q = 0; q <= j; ++q) h[q] += h2[q];
+        bem::dots64(V, N, N, j + 1, w, hbuf + 32 * pass, st);
+        bem::sub_vh64(V, N, N, j + 1, hbuf + 32 * pass, w, st);
       }
-      double hn = std::sqrt(dev_dot(c, w, w, N, hbuf));
+      bem::dots64(w, N, N, 1, w, hbuf + 62, st);
+      bem::scale_by_norm64(w, hbuf + 62, V + (size_t)(j + 1) * N, N, st);
+      double hh[64];
+      cudaMemcpyAsync(hh, hbuf, sizeof(double) * 64, cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      std::vector<double> h(j + 2, 0.0);
+      for (int q = 0; q <= j; ++q) h[q] = hh[q] + hh[32 + q];
+      const double hn = hh[62] > 0.0 ? std::sqrt(hh[62]) : 0.0;
       h[j + 1] = hn;
-      if (hn > 0) bem::scale_copy64(w, 1.0 / hn, V + (size_t)(j + 1) * N, N, st);
       // Givens
       for (int q = 0; q < j; ++q) {
         double t = cg[q] * h[q] + sg[q] * h[q + 1];
