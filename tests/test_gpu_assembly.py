@@ -196,3 +196,38 @@ def test_invalid_arguments_raise():
     dad.properties = Laplace(k=-1.0)
     with pytest.raises(BemError):
         H_G_gpu(dad)
+
+
+def test_full_size_parity_within_reference_rounding_sensitivity(orc):
+    """At the full C2 size (2731 quadratic elements, N = 8193) the reference's
+    tanp3c map is ill-conditioned for points on the adjacent element (pole just
+    outside [-1, 1], nearly collinear): a 1-ulp change of the collocation point
+    moves such entries of the FP64 oracle itself by up to ~5e-5 relative.  Every
+    GPU entry that differs from the oracle by more than 1e-10 of the largest
+    entry must lie within 10x that spread, measured per pair on the oracle."""
+    import os
+    dad = star_domain(2731, p=2, seed=0)
+    H, G = H_G_gpu(dad, T=np.float64, npg=16, near="gpu", store=False)
+    Ho, Go = orc.assemble(dad, npg=16, threads=os.cpu_count() or 1, store=False)
+    pts = np.asarray(dad.collocation)
+    rng = np.random.default_rng(3)
+    for X, Y, which in ((H, Ho, 0), (G, Go, 1)):
+        D = np.abs(X - Y)
+        bar = 1e-10 * np.max(np.abs(Y))
+        rows, cols = np.nonzero(D > bar)
+        if which == 0:
+            # H_ii is the row sum: its difference is bounded by the row's
+            diag = rows == cols
+            for r in rows[diag]:
+                assert D[r, r] <= 1.0001 * (D[r].sum() - D[r, r]) + bar
+            rows, cols = rows[~diag], cols[~diag]
+        order = np.argsort(D[rows, cols])[::-1][:12]  # the largest differences
+        for r, c in zip(rows[order], cols[order]):
+            e = c // 3
+            assert np.min(np.linalg.norm(pts[3 * e:3 * e + 3] - pts[r], axis=1)) < 1.5 * dad.elem_length[e]
+            vals = [Y[r, c], orc.integrate_element(dad, e, pts[r].copy(), source=r, npg=16)[which][c - 3 * e]]
+            for _ in range(6):
+                pp = pts[r] * (1 + rng.choice([-1.0, 1.0], 2) * 2.0 ** -52)
+                vals.append(orc.integrate_element(dad, e, pp, source=r, npg=16)[which][c - 3 * e])
+            spread = max(vals) - min(vals)
+            assert D[r, c] <= 10 * spread + bar, (which, r, c, D[r, c], spread)
