@@ -39,12 +39,13 @@ namespace tc {
 constexpr int BM = 128;
 constexpr int BN = 256;
 #define BEM_TC_BK 16
-// k chunk: one swizzle atom of FP32, 128-byte swizzle for 32, 64-byte for 16
+// k chunk: one swizzle atom of FP32, 128-byte swizzle for 32, 64-byte for
+// 16, 32-byte for 8
 constexpr int BK = BEM_TC_BK;
-static_assert(BK == 32 || BK == 16, "BK must be 16 or 32");
+static_assert(BK == 32 || BK == 16 || BK == 8, "BK must be 8, 16 or 32");
 constexpr int SW_BYTES = BK * 4;           // swizzle span (bytes per row)
 constexpr int SW_SBO = 8 * SW_BYTES;       // 8-row group stride in shared memory
-constexpr uint64_t SW_LAYOUT = BK == 32 ? 2 : 4;  // descriptor layout: 128B / 64B swizzle
+constexpr uint64_t SW_LAYOUT = BK == 32 ? 2 : (BK == 16 ? 4 : 6);  // descriptor: 128B / 64B / 32B swizzle
 #define BEM_TC_STAGES 2
 #define BEM_TC_WARPS 4
 constexpr int STAGES = BEM_TC_STAGES;
@@ -386,7 +387,9 @@ static bool make_map(CUtensorMap* m, const float* base, uint64_t inner, uint64_t
   cuuint32_t box[2] = {(cuuint32_t)tc::BK, box_outer};
   cuuint32_t es[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, tc::BK == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE,
+            tc::BK == 32 ? CU_TENSOR_MAP_SWIZZLE_128B
+                         : (tc::BK == 16 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B),
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
