@@ -17,6 +17,7 @@ BEM_SOLVE_FP64, BEM_SOLVE_MIXED = 0, 1
 BEM_OPT_TCGEN05 = 1
 BEM_OPT_KERNEL_TIMING = 2
 BEM_OPT_FAR_DF = 3
+BEM_OPT_GRAPHS = 4
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
                   "lu_panels", "lu_thin"]
 

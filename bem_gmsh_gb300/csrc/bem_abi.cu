@@ -222,6 +222,7 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   if (c->asm_join2) cudaEventDestroy(c->asm_join2);
   if (c->asm_stream) cudaStreamDestroy(c->asm_stream);
   if (c->asm_stream2) cudaStreamDestroy(c->asm_stream2);
+  if (c->lu_graph) cudaGraphExecDestroy(c->lu_graph);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
   if (c->inv_done) cudaEventDestroy(c->inv_done);

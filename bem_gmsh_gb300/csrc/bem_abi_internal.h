@@ -32,6 +32,13 @@ struct bem_ctx {
   int pair_cap_hint = 0;
   int opt_tcgen05 = 1;  // BEM_OPT_TCGEN05: trailing updates on tcgen05
   int opt_far_df = 1;   // BEM_OPT_FAR_DF
+  int opt_graphs = 1;   // BEM_OPT_GRAPHS
+  // captured factorization of the mixed solve, replayed while the buffers and
+  // sizes in its key are unchanged (captured on the second call with a key)
+  cudaGraphExec_t lu_graph = nullptr;
+  std::vector<const void*> lu_graph_key;
+  long long lu_graph_launches = 0;
+  int lu_graph_calls = 0;
   void* cusolver_handle = nullptr;  // FP64 comparison path (created on first use)
   std::vector<bem_ctx*> workers;    // sub-contexts of batched calls (own streams)
   // side stream and events of the assembly (created on first use)

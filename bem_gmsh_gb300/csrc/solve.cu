@@ -141,18 +141,69 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       bem::tc_plan(tcp[h], A32, Npad, Npad, Lt, Ltlo, Ulo);
     }
   }
+  const bool lookahead = use_tc && tcp[0].ok && tcp[1].ok;
+  // the whole factorization as one launch sequence (equilibration, LU,
+  // sweep couplings)
+  auto factor = [&]() -> int {
+    cudaMemsetAsync(info, 0, 2 * sizeof(int), st);
+    bem::lu_prepare(A64, lda, N, Npad, cs, A32, Npad, st);
+    int r;
+    if (lookahead)
+      r = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
+                                   c->events.data(), c->events.data() + K, c->thin_stream,
+                                   c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, werr);
+    else
+      r = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
+    if (r) return r;
+    bem::lu_couplings(A32, Npad, Npad, Dinv, Mc, st);
+    return 0;
+  };
+  // A CUDA graph of that sequence (four streams, ~10 launches per LU step)
+  // replaces its launches from the second call with the same buffers on:
+  // the replay removes the host launch gaps between dependent kernels of
+  // the critical chain.  Its kernel arguments (tensor maps included) are
+  // fixed at capture, hence the key.
+  const std::vector<const void*> key = {A64, (const void*)(intptr_t)lda, (const void*)(intptr_t)N, A32, cs, Dinv,
+                                        Mc, info, tcp[0].Lt, tcp[0].Ltlo, tcp[0].Ulo, tcp[1].Lt, tcp[1].Ltlo,
+                                        tcp[1].Ulo, st, (const void*)(intptr_t)lookahead};
+  const bool graphs = c->opt_graphs && lookahead && !c->prof.on;
+  if (graphs && c->lu_graph_key != key) {
+    if (c->lu_graph) cudaGraphExecDestroy(c->lu_graph);
+    c->lu_graph = nullptr;
+    c->lu_graph_key = key;
+    c->lu_graph_calls = 0;
+  }
+  ++c->lu_graph_calls;
+  int rc = 0;
+  if (graphs && !c->lu_graph && c->lu_graph_calls >= 2) {
+    const long long l0 = bem::g_launches.load();
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      rc = factor();
+      ce = cudaStreamEndCapture(st, &g);
+    }
+    if (ce == cudaSuccess && rc == 0 && g) ce = cudaGraphInstantiate(&c->lu_graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (ce != cudaSuccess || rc != 0) {
+      // capture is an optimisation: fall back to direct launches
+      c->lu_graph = nullptr;
+      c->opt_graphs = 0;
+      cudaGetLastError();
+      rc = 0;
+    }
+    c->lu_graph_launches = bem::g_launches.load() - l0;
+    bem::g_launches.fetch_sub(c->lu_graph_launches);  // counted when replayed
+  }
   tf.start(st);
-  cudaMemsetAsync(info, 0, 2 * sizeof(int), st);
-  bem::lu_prepare(A64, lda, N, Npad, cs, A32, Npad, st);
-  int rc;
-  if (use_tc && tcp[0].ok && tcp[1].ok)
-    rc = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
-                                  c->events.data(), c->events.data() + K,
-                                  c->thin_stream, c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, werr);
-  else
-    rc = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
+  if (graphs && c->lu_graph) {
+    cudaError_t ce = cudaGraphLaunch(c->lu_graph, st);
+    if (ce != cudaSuccess) return c->cuda_fail(ce, "factorization graph");
+    bem::count_launches(c->lu_graph_launches);
+  } else {
+    rc = factor();
+  }
   if (rc) return c->cuda_fail((cudaError_t)rc, "lu_factor");
-  bem::lu_couplings(A32, Npad, Npad, Dinv, Mc, st);
   tf.stop(st);
   int hinfo2[2] = {0, 0};
   cudaMemcpyAsync(hinfo2, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -436,6 +487,10 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   if (option == BEM_OPT_FAR_DF) {
     if (value < 0 || value > 2) return BEM_ERR_INVALID;
     c->opt_far_df = value;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_GRAPHS) {
+    c->opt_graphs = value ? 1 : 0;
     return BEM_OK;
   }
   return BEM_ERR_INVALID;

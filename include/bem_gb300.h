@@ -50,17 +50,24 @@ extern "C" {
 #define BEM_OPT_FAR_DF 3        /* far-field Laplace entries of FP64 systems evaluated in double-float
                                    (FP32 pairs, ~1e-14 relative): 0 never, 1 (default) in mixed-precision
                                    solves, 2 also in bem_assemble_system2d.  Kelvin stays FP64. */
+#define BEM_OPT_GRAPHS 4        /* 1 (default): the mixed solve's factorization (equilibration, look-ahead
+                                   LU, sweep couplings) is captured in a CUDA graph on the second call with
+                                   unchanged buffers and replayed; 0: direct launches.  Not used while
+                                   BEM_OPT_KERNEL_TIMING is on. */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */
 #define BEM_KC_NEAR 1      /* near-singular, on-element and diagonal kernels */
 #define BEM_KC_LU_PREP 2   /* equilibration + FP32 copy */
-#define BEM_KC_LU_CRIT 3   /* LU critical path: diagonal blocks, panels, thin updates */
+#define BEM_KC_LU_CRIT 3   /* LU critical path: diagonal blocks and panels */
 #define BEM_KC_LU_TRAIL 4  /* LU bulk trailing updates (tcgen05) */
 #define BEM_KC_TRSV 5      /* triangular solves of the preconditioner */
 #define BEM_KC_GEMV 6      /* FP64 matrix-vector products and residuals */
 #define BEM_KC_LU_TOTAL 7  /* whole factorization */
-#define BEM_KC_COUNT 8
+#define BEM_KC_LU_DIAG 8   /* diagonal-block factorizations (part of BEM_KC_LU_CRIT) */
+#define BEM_KC_LU_PANELS 9 /* panel triangular solves (part of BEM_KC_LU_CRIT) */
+#define BEM_KC_LU_THIN 10  /* look-ahead thin updates (own stream) */
+#define BEM_KC_COUNT 11
 
 /* solve modes */
 #define BEM_SOLVE_FP64 0  /* FP64 assembly + FP64 LU */
