@@ -815,6 +815,22 @@ __device__ __forceinline__ float rcp_nr(float x) {
   return fmaf(r, fmaf(-x, r, 1.f), r);
 }
 
+// x = hi + lo with hi = tf32(x) (round to nearest) and lo = tf32(x - hi)
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+  const float r = x - __uint_as_float(hi);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+// d += a b, one m16n8k8 TF32 tile (A row-major fragment, B column-major)
+__device__ __forceinline__ void mma_tf32_16x8x8(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64_t ld, int k,
                                                  float* __restrict__ SI, int* __restrict__ info, int pre) {
   extern __shared__ __align__(16) float dsm[];
@@ -844,12 +860,15 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
     }
   }
   if (pre && k > 0) {
-    // A_kk -= L_{k,k-1} U_{k-1,k}: thread -> rows 4 (t % 32) .. +3,
-    // columns 8 (t / 32) .. +7
+    // A_kk -= L_{k,k-1} U_{k-1,k} on the tensor cores: mma.sync m16n8k8
+    // TF32 with the split x = hi + lo (hi = tf32(x)) and three products
+    // hi*hi + hi*lo + lo*hi (FP32-level accuracy).  Warp w owns rows
+    // 32 (w % 4) .. +31 and columns 32 (w / 4) .. +31: 2 x 4 tiles of 16 x 8.
     const float* Lb = Ab - LU_NB * ld;  // block (k, k-1)
     const float* Ub = Ab - LU_NB;       // block (k-1, k)
-    const int r0 = 4 * (t & 31), c0 = 8 * (t >> 5);
-    float acc[4][8] = {};
+    const int g = lane >> 2, tq = lane & 3;
+    const int rw = 32 * (warp & 3), cw = 32 * (warp >> 2);
+    float acc[2][4][4] = {};
     for (int kc = 0; kc < LU_NB; kc += PRE_KC) {
       __syncthreads();
 #pragma unroll
@@ -860,25 +879,45 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
         *(float4*)&Uc[c * PRE_ULD + q4] = __ldcg((const float4*)(Ub + kc + q4 + (size_t)c * ld));
       }
       __syncthreads();
-#pragma unroll 4
-      for (int q = 0; q < PRE_KC; ++q) {
-        const float4 a = *(const float4*)&Lc[q * TLD + r0];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const float b = Uc[(c0 + j) * PRE_ULD + q];
-          acc[0][j] = fmaf(a.x, b, acc[0][j]);
-          acc[1][j] = fmaf(a.y, b, acc[1][j]);
-          acc[2][j] = fmaf(a.z, b, acc[2][j]);
-          acc[3][j] = fmaf(a.w, b, acc[3][j]);
+      for (int ks = 0; ks < PRE_KC; ks += 8) {
+        uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+          const int r = rw + 16 * mt + g;
+          const float av[4] = {Lc[(ks + tq) * TLD + r], Lc[(ks + tq) * TLD + r + 8], Lc[(ks + tq + 4) * TLD + r],
+                               Lc[(ks + tq + 4) * TLD + r + 8]};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) split_tf32(av[e], ah[mt][e], al[mt][e]);
         }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          const int c = cw + 8 * nt + g;
+          const float bv[2] = {Uc[c * PRE_ULD + ks + tq], Uc[c * PRE_ULD + ks + tq + 4]};
+#pragma unroll
+          for (int e = 0; e < 2; ++e) split_tf32(bv[e], bh[nt][e], bl[nt][e]);
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < 4; ++nt) {
+            mma_tf32_16x8x8(acc[mt][nt], al[mt], bh[nt]);
+            mma_tf32_16x8x8(acc[mt][nt], ah[mt], bl[nt]);
+            mma_tf32_16x8x8(acc[mt][nt], ah[mt], bh[nt]);
+          }
       }
     }
+    // accumulator layout: c0 (g, 2 tq), c1 (g, 2 tq + 1), c2 (g + 8, 2 tq), c3 (g + 8, 2 tq + 1)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float4 v = *(float4*)&S[(c0 + j) * TLD + r0];
-      v.x -= acc[0][j]; v.y -= acc[1][j]; v.z -= acc[2][j]; v.w -= acc[3][j];
-      *(float4*)&S[(c0 + j) * TLD + r0] = v;
-    }
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int r = rw + 16 * mt + g, c = cw + 8 * nt + 2 * tq;
+        S[c * TLD + r] -= acc[mt][nt][0];
+        S[(c + 1) * TLD + r] -= acc[mt][nt][1];
+        S[c * TLD + r + 8] -= acc[mt][nt][2];
+        S[(c + 1) * TLD + r + 8] -= acc[mt][nt][3];
+      }
   }
   __syncthreads();
   int bad = 0;
