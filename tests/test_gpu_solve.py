@@ -142,3 +142,17 @@ def test_factorization_graph_replay_matches_direct_launches():
             assert rel(x, x_direct) < 1e-12
     finally:
         ctx.close()
+
+
+def test_large_system_uses_stepwise_sweeps():
+    """N = 20100 (157 block rows, more than the co-resident CTAs of the
+    wavefront sweep): the preconditioner falls back to step-wise sweeps and
+    the mixed solve still matches the FP64 path."""
+    dad = star_domain(6700, p=2, seed=2)
+    assert dad.nt == 20100
+    _, st = solve(dad, npg=16, mode="mixed", return_stats=True)
+    x_mixed = dad.cache["x"].copy()
+    ref = star_domain(6700, p=2, seed=2)
+    solve(ref, npg=16, mode="fp64")
+    assert rel(x_mixed, ref.cache["x"]) < 1e-10, st
+    assert st["rel_residual"] <= 1e-14, st
