@@ -105,13 +105,15 @@ def cpu_reference(dad_factory, steps, warmup, npg):
     from oracle import oracle as orc
     ts = []
     x = None
+    stages = {}
     for it in range(warmup + steps):
         dad = dad_factory()
         r = orc.timed_pipeline(dad, npg=npg, threads=os.cpu_count() or 1)
         if it >= warmup:
             ts.append(r["total"])
         x = r["x"]
-    return ts, x
+        stages = {k: r[k] for k in ("assemble", "apply_bc", "lu")}
+    return ts, x, stages
 
 
 # DRAM traffic of one bulk trailing update (k_gemm_tc) at the C2 trailing size,
@@ -234,7 +236,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        ts, _ = cpu_reference(make, max(1, args.steps), min(args.warmup, 1), args.npg)
+        ts, _, _ = cpu_reference(make, max(1, args.steps), min(args.warmup, 1), args.npg)
         v = 1.0 / statistics.mean(ts)
         cores = os.cpu_count() or 1
         line = {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": len(ts),
@@ -354,6 +356,25 @@ def main():
     ms_asm = a0.elapsed_time(a1) / args.steps
     entries = N * N + N * dad.n
     entries_per_s = entries / (ms_asm * 1e-3)
+    del Hs, Gs
+    # the same H, G in FP64 (the FP64 comparison path's assembly)
+    Hd = torch.empty((N, ld), dtype=torch.float64, device="cuda")
+    Gd = torch.empty((dad.n, ld), dtype=torch.float64, device="cuda")
+
+    def asm64():
+        rc = ctx.L.bem_assemble_laplace2d(ctx.h, g, 1.0, args.npg, 1.5, _lib.BEM_F64, _lib.BEM_MEM_DEVICE,
+                                          Hd.t()[:N].data_ptr(), ld, Gd.t()[:N].data_ptr(), ld)
+        ctx.check(rc, "assemble fp64")
+    asm64()
+    torch.cuda.synchronize()
+    a0.record(stream)
+    n64 = max(1, min(args.steps, 5))
+    for _ in range(n64):
+        asm64()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    ms_asm64 = a0.elapsed_time(a1) / n64
+    del Hd, Gd
 
     # end to end through the public API (host buffers)
     ctx.set_stream(0)
@@ -430,10 +451,15 @@ def main():
         extra = extra_configs(ctx)
 
     # CPU baseline: the oracle port on the host cores, one full solve sample
-    cpu_ts, x_orc = cpu_reference(make, max(1, args.cpu_samples), 0, args.npg)
+    cpu_ts, x_orc, cpu_stages = cpu_reference(make, max(1, args.cpu_samples), 0, args.npg)
     cores = os.cpu_count() or 1
     cpu_v = 1.0 / statistics.mean(cpu_ts)
     rel_vs_oracle = float(np.linalg.norm(x_mixed - x_orc) / np.linalg.norm(x_orc))
+
+    def analytic_error(x):
+        d = make()
+        split_sol(d, x)
+        return float(rel_error(d))
 
     if rank == 0:
         line = {
@@ -448,6 +474,13 @@ def main():
             "speedup_mixed_vs_fp64": ms64 / ms,
             "rel_err_vs_fp64_gpu": rel_vs_fp64, "rel_err_vs_cpu_oracle": rel_vs_oracle,
             "rel_error_analytic": float(rel_error(e2e_dad)),
+            "rel_error_analytic_fp64_gpu": analytic_error(x64),
+            "rel_error_analytic_cpu": analytic_error(x_orc),
+            "fp64_assembly_ms_HG": ms_asm64, "fp64_entries_per_s": entries / (ms_asm64 * 1e-3),
+            "cpu_stages": {"assembly_ms": 1e3 * cpu_stages["assemble"],
+                           "entries_per_s": entries / cpu_stages["assemble"],
+                           "apply_bc_ms": 1e3 * cpu_stages["apply_bc"], "lu_ms": 1e3 * cpu_stages["lu"],
+                           "note": "oracle assembly on all host threads, LAPACK LU"},
             "gmres_iterations": iters[-1] if iters else None, "stats": stats_mixed,
             "kernel_ms_per_step": {k: v[0] / prof_steps for k, v in ktimes.items()},
             "e2e": {"value": 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),

@@ -44,11 +44,18 @@ def test_solve_system_device_pointers():
     assert rel(x.cpu().numpy(), np.linalg.solve(A, b)) < 1e-12
 
 
+# C1: the reference's unit square (19 linear elements per side, left T = 0,
+# right q = -1); C1': 20 elements per side with T prescribed on left (0) and
+# right (1), q = 0 on top and bottom
+C1_CASES = {"C1": dict(ndiv=20), "C1prime": dict(ndiv=21, bcs={"right": (0, 1.0)})}
+
+
+@pytest.mark.parametrize("case", sorted(C1_CASES))
 @pytest.mark.parametrize("mode", ["mixed", "fp64"])
-def test_quadrado_pipeline(orc, mode):
-    dad = quadrado(ndiv=20, pontointerno=True)
+def test_quadrado_pipeline(orc, mode, case):
+    dad = quadrado(pontointerno=True, **C1_CASES[case])
     attach_analytical(dad, ana_laplace_linear())
-    ref = quadrado(ndiv=20, pontointerno=True)
+    ref = quadrado(pontointerno=True, **C1_CASES[case])
     attach_analytical(ref, ana_laplace_linear())
     orc.assemble(ref, npg=20)
     orc.solve(ref)
