@@ -160,18 +160,13 @@ bool bem_ctx::lookahead_ready(int k) {
     }
     if (cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming) != cudaSuccess) return false;
   }
-  if (!inv_stream) {
+  if (!thin_stream) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    if (cudaStreamCreateWithFlags(&inv_stream, cudaStreamNonBlocking) != cudaSuccess) {
-      inv_stream = nullptr;
-      return false;
-    }
     if (cudaStreamCreateWithPriority(&thin_stream, cudaStreamNonBlocking, hi) != cudaSuccess) {
       thin_stream = nullptr;
       return false;
     }
-    if (cudaEventCreateWithFlags(&inv_done, cudaEventDisableTiming) != cudaSuccess) return false;
   }
   while ((int)events.size() < 3 * k) {
     cudaEvent_t e;
@@ -225,8 +220,6 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   if (c->lu_graph) cudaGraphExecDestroy(c->lu_graph);
   if (c->fork_event) cudaEventDestroy(c->fork_event);
   if (c->la_stream) cudaStreamDestroy(c->la_stream);
-  if (c->inv_done) cudaEventDestroy(c->inv_done);
-  if (c->inv_stream) cudaStreamDestroy(c->inv_stream);
   if (c->thin_stream) cudaStreamDestroy(c->thin_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;

@@ -50,10 +50,8 @@ struct bem_ctx {
   cudaStream_t la_stream = nullptr;
   cudaEvent_t fork_event = nullptr;
   std::vector<cudaEvent_t> events;
-  // third and fourth streams of the lookahead LU (diagonal-block inverses,
-  // thin updates)
-  cudaStream_t inv_stream = nullptr, thin_stream = nullptr;
-  cudaEvent_t inv_done = nullptr;
+  // third stream of the lookahead LU (thin updates)
+  cudaStream_t thin_stream = nullptr;
   // Ensures 3*k events and the lookahead streams; false on failure.
   bool lookahead_ready(int k);
 

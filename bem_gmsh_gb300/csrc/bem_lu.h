@@ -76,7 +76,6 @@ void tc_split(const TcPlan& p, int k, cudaStream_t st);
 int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st);
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        cudaStream_t tl, cudaEvent_t* evR, cudaStream_t iv, cudaEvent_t ivdone,
-                        const TcPlan* tc, int* err);
+                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err);
 
 }  // namespace bem

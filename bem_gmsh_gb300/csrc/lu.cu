@@ -1098,11 +1098,17 @@ __device__ __forceinline__ void cp_async_wait_all() {
 //     For each sub-block p: X_p = B_p Uinv_pp, then B_q -= X_p U_pq (q > p).
 // ident: the slices start as the corresponding part of the identity (not
 // read), which gives the full inverses L^{-1} and U^{-1} of the block for the
-// triangular sweeps.  B and Ap have leading dimension ld.
+// triangular sweeps.  B and Ap have leading dimension ld.  blockIdx.z
+// offsets Dk, SIk and B/Ap by z times zsD, zsSI and zsX (all diagonal blocks
+// in one launch).
 __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, int64_t ldk,
                                                 const float* __restrict__ SIk, float* B, float* Ap, int64_t ld,
-                                                int ident) {
+                                                int ident, int64_t zsD, int64_t zsSI, int64_t zsX) {
   extern __shared__ __align__(16) float psm[];
+  Dk += blockIdx.z * zsD;
+  SIk += blockIdx.z * zsSI;
+  B += blockIdx.z * zsX;
+  Ap += blockIdx.z * zsX;
   float* Ms = psm;                   // factored block, column-major, ld TLD
   float* Xs = psm + LU_NB * TLD;     // the slice
   float* Si = Xs + LU_NB * PXLD;     // [p][16 x 16], column-major
@@ -1367,17 +1373,18 @@ static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStrea
   float* A21 = A + (kk + LU_NB) + kk * ld;
   KScope kp(st, KC_LU_PANELS);
   k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k), A12,
-                                                       A21, ld, 0);
+                                                       A21, ld, 0, 0, 0, 0);
   count_launches(1);
 }
 
-// the full inverses of the unit-lower and upper triangles of diagonal block
-// k into Dinv (for the triangular sweeps; off the factorization's chain)
-static void block_inverses(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st) {
-  const size_t kk = (size_t)k * LU_NB;
-  float* Lo = Dinv + (size_t)k * 2 * LU_NB * LU_NB;
-  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k), Lo,
-                                                         Lo + LU_NB * LU_NB, LU_NB, 1);
+// the full inverses of the unit-lower and upper triangles of diagonal blocks
+// k0 .. k0 + nk - 1 into Dinv (for the triangular sweeps), one launch
+static void block_inverses(float* A, int64_t ld, int Npad, float* Dinv, int k0, int nk, cudaStream_t st) {
+  const size_t kk = (size_t)k0 * LU_NB;
+  float* Lo = Dinv + (size_t)k0 * 2 * LU_NB * LU_NB;
+  k_panels<<<dim3(LU_NB / PW, 2, nk), 256, PANEL_SMEM, st>>>(
+      A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k0), Lo, Lo + LU_NB * LU_NB, LU_NB, 1,
+      (int64_t)LU_NB * (ld + 1), LU_SI, 2 * LU_NB * LU_NB);
   count_launches(1);
 }
 
@@ -1387,7 +1394,7 @@ static void diag_and_panels(float* A, int64_t ld, int Npad, float* Dinv, int* in
   (void)x3;
   diag_block(A, ld, Npad, Dinv, info, k, st);
   panels(A, ld, Npad, Dinv, k, st);
-  block_inverses(A, ld, Npad, Dinv, k, st);
+  block_inverses(A, ld, Npad, Dinv, k, 1, st);
 }
 
 int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cudaStream_t st,
@@ -1414,20 +1421,18 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
   return (int)cudaGetLastError();
 }
 
-// Lookahead-1 schedule on four streams.  `la` (the critical path) factors
+// Lookahead-1 schedule on three streams.  `la` (the critical path) factors
 // diagonal block k+1, applying step k's update to that block itself, then
 // its panels; `tl` meanwhile applies the rest of step k's thin update (block
 // column k+1 below the diagonal block and block row k+1 right of it, FP32);
 // `st` splits step k's panels into the tensor-core operands and runs the
-// bulk of step k's trailing update; `iv` forms the full inverses of each
-// diagonal block once its panels are done.  evP[k]: panels of step k ready;
-// evT[k]: bulk update of step k done; evR[k]: thin update of step k done;
-// ivdone: all inverses formed.  tc[2]: plans with separate lo/transposed
-// buffers for even and odd steps.
+// bulk of step k's trailing update, and at the end forms the full inverses
+// of all diagonal blocks in one launch.  evP[k]: panels of step k ready;
+// evT[k]: bulk update of step k done; evR[k]: thin update of step k done.
+// tc[2]: plans with separate lo/transposed buffers for even and odd steps.
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        cudaStream_t tl, cudaEvent_t* evR, cudaStream_t iv, cudaEvent_t ivdone,
-                        const TcPlan* tc, int* err) {
+                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err) {
   const int K = Npad / LU_NB;
   lu_attrs();
   KScope total(st, KC_LU_TOTAL);
@@ -1436,8 +1441,6 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
   diag_block(A, ld, Npad, Dinv, info, 0, la);
   panels(A, ld, Npad, Dinv, 0, la);
   cudaEventRecord(evP[0], la);
-  cudaStreamWaitEvent(iv, evP[0], 0);
-  block_inverses(A, ld, Npad, Dinv, 0, iv);
   for (int k = 0; k + 1 < K; ++k) {
     const int rem = Npad - (k + 1) * LU_NB;
     const TcPlan& P = tc[k & 1];
@@ -1455,8 +1458,6 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
       panels(A, ld, Npad, Dinv, k + 1, la);
     }
     cudaEventRecord(evP[k + 1], la);
-    cudaStreamWaitEvent(iv, evP[k + 1], 0);
-    block_inverses(A, ld, Npad, Dinv, k + 1, iv);
     cudaStreamWaitEvent(st, evP[k], 0);
     if (rem > LU_NB) {
       KScope trail(st, KC_LU_TRAIL);
@@ -1467,8 +1468,8 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     cudaEventRecord(evT[k], st);
   }
   cudaStreamWaitEvent(st, evP[K - 1], 0);
-  cudaEventRecord(ivdone, iv);
-  cudaStreamWaitEvent(st, ivdone, 0);
+  // all block inverses in one launch once the factorization is done
+  block_inverses(A, ld, Npad, Dinv, 0, K, st);
   return (int)cudaGetLastError();
 }
 
@@ -1613,7 +1614,7 @@ void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float
                    cudaStream_t st) {
   lu_attrs();
   k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info, 0);
-  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1);
+  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1, 0, 0, 0);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
   count_launches(3);
 }

@@ -142,8 +142,8 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
     }
   }
   const bool lookahead = use_tc && tcp[0].ok && tcp[1].ok;
-  // the whole factorization as one launch sequence (equilibration, LU,
-  // sweep couplings)
+  // the whole factorization as one launch sequence (equilibration, LU, block
+  // inverses, sweep couplings)
   auto factor = [&]() -> int {
     cudaMemsetAsync(info, 0, 2 * sizeof(int), st);
     bem::lu_prepare(A64, lda, N, Npad, cs, A32, Npad, st);
@@ -151,14 +151,14 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
     if (lookahead)
       r = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
                                    c->events.data(), c->events.data() + K, c->thin_stream,
-                                   c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, werr);
+                                   c->events.data() + 2 * K, tcp, werr);
     else
       r = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
     if (r) return r;
     bem::lu_couplings(A32, Npad, Npad, Dinv, Mc, st);
     return 0;
   };
-  // A CUDA graph of that sequence (four streams, ~10 launches per LU step)
+  // A CUDA graph of that sequence (three streams, ~8 launches per LU step)
   // replaces its launches from the second call with the same buffers on:
   // the replay removes the host launch gaps between dependent kernels of
   // the critical chain.  Its kernel arguments (tensor maps included) are
@@ -620,7 +620,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   t1.start(st);
   int rc = bem::lu_factor_lookahead(A1, n, n, Dinv, info, st, c->la_stream, c->fork_event,
                                     c->events.data(), c->events.data() + K,
-                                  c->thin_stream, c->events.data() + 2 * K, c->inv_stream, c->inv_done, tcp, info + 1);
+                                  c->thin_stream, c->events.data() + 2 * K, tcp, info + 1);
   t1.stop(st);
   if (rc) return c->cuda_fail((cudaError_t)rc, "selftest tcgen05 LU");
   t2.start(st);
