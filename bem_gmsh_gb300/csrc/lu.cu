@@ -1100,10 +1100,19 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // read), which gives the full inverses L^{-1} and U^{-1} of the block for the
 // triangular sweeps.  B and Ap have leading dimension ld.  blockIdx.z
 // offsets Dk, SIk and B/Ap by z times zsD, zsSI and zsX (all diagonal blocks
-// in one launch).
+// in one launch).  When Lt is given, the kernel also writes the operands of
+// the step's tensor-core trailing update: Lt / Ltlo = L21 and its TF32 low
+// part x - tf32(x), row-major [row][k] (rows counted from the first row
+// below the block), and Ulo = the low part of U12, [column][k].
+__device__ __forceinline__ float tf32_low(float x) {
+  return x - __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+
 __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, int64_t ldk,
                                                 const float* __restrict__ SIk, float* B, float* Ap, int64_t ld,
-                                                int ident, int64_t zsD, int64_t zsSI, int64_t zsX) {
+                                                int ident, int64_t zsD, int64_t zsSI, int64_t zsX,
+                                                float* __restrict__ Lt, float* __restrict__ Ltlo,
+                                                float* __restrict__ Ulo) {
   extern __shared__ __align__(16) float psm[];
   Dk += blockIdx.z * zsD;
   SIk += blockIdx.z * zsSI;
@@ -1187,7 +1196,11 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int idx = t + 256 * i, r4 = 4 * (idx & 31), c = idx >> 5;
-      *(float4*)&Bb[r4 + (size_t)c * ld] = *(const float4*)&Xs[c * TLD + r4];
+      const float4 v = *(const float4*)&Xs[c * TLD + r4];
+      *(float4*)&Bb[r4 + (size_t)c * ld] = v;
+      if (Ulo)
+        *(float4*)&Ulo[(size_t)(blockIdx.x * PW + c) * LU_NB + r4] =
+            make_float4(tf32_low(v.x), tf32_low(v.y), tf32_low(v.z), tf32_low(v.w));
     }
   } else {
     // slice [col][row], ld PXLD: Xs[c * PXLD + r], 32 rows
@@ -1248,6 +1261,20 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
     for (int i = 0; i < 4; ++i) {
       const int idx = t + 256 * i, r4 = 4 * (idx & 7), c = idx >> 3;
       *(float4*)(Ab + r4 + (size_t)c * ld) = *(const float4*)&Xs[c * PXLD + r4];
+    }
+    if (Lt) {
+      // row-major copies for the tensor-core operands: thread -> row t / 8,
+      // columns 4 (t % 8) + 32 j
+      const int rr = t >> 3, c4 = 4 * (t & 7);
+      const size_t row = (size_t)blockIdx.x * PW + rr;
+#pragma unroll
+      for (int j = 0; j < LU_NB / 32; ++j) {
+        const int c = 32 * j + c4;
+        const float4 v = make_float4(Xs[c * PXLD + rr], Xs[(c + 1) * PXLD + rr], Xs[(c + 2) * PXLD + rr],
+                                     Xs[(c + 3) * PXLD + rr]);
+        *(float4*)&Lt[row * LU_NB + c] = v;
+        *(float4*)&Ltlo[row * LU_NB + c] = make_float4(tf32_low(v.x), tf32_low(v.y), tf32_low(v.z), tf32_low(v.w));
+      }
     }
   }
 }
@@ -1364,8 +1391,10 @@ static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, i
   count_launches(1);
 }
 
-// the two panels of diagonal block k: U12 = L^{-1} A12, L21 = A21 U^{-1}
-static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st) {
+// the two panels of diagonal block k: U12 = L^{-1} A12, L21 = A21 U^{-1};
+// with a plan, also the step's tensor-core operands (Lt, Ltlo, Ulo)
+static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStream_t st,
+                   const TcPlan* P = nullptr) {
   const size_t kk = (size_t)k * LU_NB;
   const int rem = Npad - (int)kk - LU_NB;
   if (rem <= 0) return;
@@ -1373,7 +1402,8 @@ static void panels(float* A, int64_t ld, int Npad, float* Dinv, int k, cudaStrea
   float* A21 = A + (kk + LU_NB) + kk * ld;
   KScope kp(st, KC_LU_PANELS);
   k_panels<<<dim3(rem / PW, 2), 256, PANEL_SMEM, st>>>(A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k), A12,
-                                                       A21, ld, 0, 0, 0, 0);
+                                                       A21, ld, 0, 0, 0, 0, P ? P->Lt : nullptr,
+                                                       P ? P->Ltlo : nullptr, P ? P->Ulo : nullptr);
   count_launches(1);
 }
 
@@ -1384,7 +1414,7 @@ static void block_inverses(float* A, int64_t ld, int Npad, float* Dinv, int k0, 
   float* Lo = Dinv + (size_t)k0 * 2 * LU_NB * LU_NB;
   k_panels<<<dim3(LU_NB / PW, 2, nk), 256, PANEL_SMEM, st>>>(
       A + kk + kk * ld, ld, sub_inverses(Dinv, Npad, k0), Lo, Lo + LU_NB * LU_NB, LU_NB, 1,
-      (int64_t)LU_NB * (ld + 1), LU_SI, 2 * LU_NB * LU_NB);
+      (int64_t)LU_NB * (ld + 1), LU_SI, 2 * LU_NB * LU_NB, nullptr, nullptr, nullptr);
   count_launches(1);
 }
 
@@ -1425,8 +1455,8 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
 // diagonal block k+1, applying step k's update to that block itself, then
 // its panels; `tl` meanwhile applies the rest of step k's thin update (block
 // column k+1 below the diagonal block and block row k+1 right of it, FP32);
-// `st` splits step k's panels into the tensor-core operands and runs the
-// bulk of step k's trailing update, and at the end forms the full inverses
+// `st` runs the bulk of step k's trailing update (its tensor-core operands
+// come from the panel kernel), and at the end forms the full inverses
 // of all diagonal blocks in one launch.  evP[k]: panels of step k ready;
 // evT[k]: bulk update of step k done; evR[k]: thin update of step k done.
 // tc[2]: plans with separate lo/transposed buffers for even and odd steps.
@@ -1439,7 +1469,7 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
   cudaEventRecord(fork, st);
   cudaStreamWaitEvent(la, fork, 0);
   diag_block(A, ld, Npad, Dinv, info, 0, la);
-  panels(A, ld, Npad, Dinv, 0, la);
+  panels(A, ld, Npad, Dinv, 0, la, &tc[0]);
   cudaEventRecord(evP[0], la);
   for (int k = 0; k + 1 < K; ++k) {
     const int rem = Npad - (k + 1) * LU_NB;
@@ -1455,13 +1485,13 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
       KScope crit(la, KC_LU_CRIT);
       diag_block(A, ld, Npad, Dinv, info, k + 1, la, 1);
       cudaStreamWaitEvent(la, evR[k], 0);
-      panels(A, ld, Npad, Dinv, k + 1, la);
+      panels(A, ld, Npad, Dinv, k + 1, la, &tc[(k + 1) & 1]);
     }
     cudaEventRecord(evP[k + 1], la);
     cudaStreamWaitEvent(st, evP[k], 0);
     if (rem > LU_NB) {
       KScope trail(st, KC_LU_TRAIL);
-      tc_split(P, k, st);
+      // operands Lt, Ltlo, Ulo of step k were written by its panels
       int e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
       if (e) return e;
     }
@@ -1614,7 +1644,8 @@ void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float
                    cudaStream_t st) {
   lu_attrs();
   k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info, 0);
-  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1, 0, 0, 0);
+  k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1, 0, 0, 0,
+                                                        nullptr, nullptr, nullptr);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
   count_launches(3);
 }
