@@ -240,9 +240,14 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   std::vector<double> H((m + 1) * m), cg(m), sg(m), gvec(m + 1), y(m);
   bool converged = false;
   double prev_beta = INFINITY;
+  bool x_zero = true;  // x was just zeroed: the first residual is b itself
   while (iters < max_iter && !converged) {
     // r = b - A x (FP64)
-    bem::residual64(A64, lda, N, x, b, w, st);
+    if (x_zero)
+      cudaMemcpyAsync(w, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, st);
+    else
+      bem::residual64(A64, lda, N, x, b, w, st);
+    x_zero = false;
     double beta = std::sqrt(dev_dot(c, w, w, N, hbuf));
     relres = beta / bnorm;
     if (relres <= tol) { converged = true; break; }
