@@ -414,8 +414,9 @@ def main():
                      "tcgen05 3xTF32 trailing updates (k_gemm_tc): C read + write per step"),
         # bytes: FP32 L and U read once per preconditioner application
         "trsv": ("hbm", 4.0 * nb * nb * iters_last, "GB/s", "FP32 LU read per sweep pair"),
-        # bytes: one FP64 A read per product (initial residual + one per iteration + final)
-        "gemv": ("hbm", 8.0 * N * N * (iters_last + 2), "GB/s", "FP64 A read per product"),
+        # bytes: one FP64 A read per product (one per iteration + the final
+        # residual; the first residual from x = 0 is b itself)
+        "gemv": ("hbm", 8.0 * N * N * (iters_last + 1), "GB/s", "FP64 A read per product"),
     }
     classes = {}
     for k, (bound, units, unit, note) in algo.items():
