@@ -774,7 +774,7 @@ constexpr int TLD = LU_NB + 4;  // shared leading dimension
 constexpr int PRE_KC = 32;
 constexpr int PRE_ULD = PRE_KC + 4;
 constexpr int DIAG_SMEM =
-    (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 2 * DB * DB + PRE_KC * TLD + LU_NB * PRE_ULD);
+    (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 4 * DB * DB + PRE_KC * TLD + LU_NB * PRE_ULD);
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -837,9 +837,8 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
   float* S = dsm;                       // A -> L\U
   float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
   float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
-  float* LiP = Ls + 16 * 20;            // Linv_pp, column-major, ld 16
-  float* UiP = LiP + DB * DB;           // Uinv_pp, column-major, ld 16
-  float* Lc = UiP + DB * DB;            // pre-update L chunk [q][r], ld TLD
+  float* LiP = Ls + 16 * 20;            // [parity][Linv_pp, Uinv_pp], column-major, ld 16
+  float* Lc = LiP + 4 * DB * DB;        // pre-update L chunk [q][r], ld TLD
   float* Uc = Lc + PRE_KC * TLD;        // pre-update U chunk [c][q], ld PRE_ULD
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
@@ -921,84 +920,113 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
   }
   __syncthreads();
   int bad = 0;
-  for (int p = 0; p < LU_NB / DB; ++p) {
-    const int jb = p * DB;
-    // ---- A ----
-    if (warp < 4) {
-      float PT[DB], PB[DB];
-      const int rb = jb + DB + 32 * warp + lane;
-      const bool tv = lane < DB, bv = rb < LU_NB;
+  // phase A of panel jb (warps 0-3): factor rows jb.. of columns jb..jb+15,
+  // warp 1 then inverts the unit-lower 16 x 16 block into Li
+  auto factor_panel = [&](int jb, float* Li) {
+    float PT[DB], PB[DB];
+    const int rb = jb + DB + 32 * warp + lane;
+    const bool tv = lane < DB, bv = rb < LU_NB;
 #pragma unroll
-      for (int c = 0; c < DB; ++c) {
-        PT[c] = tv ? S[(jb + c) * TLD + jb + lane] : 0.f;
-        PB[c] = bv ? S[(jb + c) * TLD + rb] : 0.f;
+    for (int c = 0; c < DB; ++c) {
+      PT[c] = tv ? S[(jb + c) * TLD + jb + lane] : 0.f;
+      PB[c] = bv ? S[(jb + c) * TLD + rb] : 0.f;
+    }
+    float* myrow = rowbuf + warp * 32;
+#pragma unroll
+    for (int c = 0; c < DB; ++c) {
+      float* rw = myrow + (c & 1) * DB;
+      if (lane == c) {
+#pragma unroll
+        for (int q4 = 0; q4 < DB; q4 += 4)
+          *(float4*)&rw[q4] = make_float4(PT[q4], PT[q4 + 1], PT[q4 + 2], PT[q4 + 3]);
       }
-      float* myrow = rowbuf + warp * 32;
+      __syncwarp();
+      float row[DB];
 #pragma unroll
-      for (int c = 0; c < DB; ++c) {
-        float* rw = myrow + (c & 1) * DB;
-        if (lane == c) {
+      for (int q4 = 0; q4 < DB; q4 += 4) {
+        const float4 v4 = *(const float4*)&rw[q4];
+        row[q4] = v4.x; row[q4 + 1] = v4.y; row[q4 + 2] = v4.z; row[q4 + 3] = v4.w;
+      }
+      const float piv = row[c];
+      if (!(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
+      const float inv = rcp_nr(piv);
+      if (lane > c && tv) {
+        const float l = PT[c] * inv;
+        PT[c] = l;
 #pragma unroll
-          for (int q4 = 0; q4 < DB; q4 += 4)
-            *(float4*)&rw[q4] = make_float4(PT[q4], PT[q4 + 1], PT[q4 + 2], PT[q4 + 3]);
-        }
-        __syncwarp();
-        float row[DB];
-#pragma unroll
-        for (int q4 = 0; q4 < DB; q4 += 4) {
-          const float4 v4 = *(const float4*)&rw[q4];
-          row[q4] = v4.x; row[q4 + 1] = v4.y; row[q4 + 2] = v4.z; row[q4 + 3] = v4.w;
-        }
-        const float piv = row[c];
-        if (!(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
-        const float inv = rcp_nr(piv);
-        if (lane > c && tv) {
-          const float l = PT[c] * inv;
-          PT[c] = l;
-#pragma unroll
-          for (int c2 = c + 1; c2 < DB; ++c2) PT[c2] = fmaf(-l, row[c2], PT[c2]);
-        }
-        if (bv) {
-          const float l = PB[c] * inv;
-          PB[c] = l;
-#pragma unroll
-          for (int c2 = c + 1; c2 < DB; ++c2) PB[c2] = fmaf(-l, row[c2], PB[c2]);
-        }
+        for (int c2 = c + 1; c2 < DB; ++c2) PT[c2] = fmaf(-l, row[c2], PT[c2]);
       }
       if (bv) {
+        const float l = PB[c] * inv;
+        PB[c] = l;
 #pragma unroll
-        for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + rb] = PB[c];
-      }
-      if (warp == 0 && tv) {
-#pragma unroll
-        for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + jb + lane] = PT[c];
-      } else if (warp == 1) {
-        // inverse of the unit-lower 16 x 16 block, lane c < 16 solving for
-        // column c by column-oriented forward substitution
-        if (tv) {
-#pragma unroll
-          for (int q = 0; q < DB; ++q) Ls[q * 20 + lane] = PT[q];
-        }
-        __syncwarp();
-        float x[DB];
-#pragma unroll
-        for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-        for (int q = 0; q < DB - 1; ++q) {
-#pragma unroll
-          for (int i = q + 1; i < DB; ++i) x[i] = fmaf(-Ls[q * 20 + i], x[q], x[i]);
-        }
-        if (tv) {
-#pragma unroll
-          for (int i4 = 0; i4 < DB; i4 += 4)
-            *(float4*)&LiP[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
-        }
+        for (int c2 = c + 1; c2 < DB; ++c2) PB[c2] = fmaf(-l, row[c2], PB[c2]);
       }
     }
-    __syncthreads();
-    // ---- B ----
+    if (bv) {
+#pragma unroll
+      for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + rb] = PB[c];
+    }
+    if (warp == 0 && tv) {
+#pragma unroll
+      for (int c = 0; c < DB; ++c) S[(jb + c) * TLD + jb + lane] = PT[c];
+    } else if (warp == 1) {
+      // inverse of the unit-lower 16 x 16 block, lane c < 16 solving for
+      // column c by column-oriented forward substitution
+      if (tv) {
+#pragma unroll
+        for (int q = 0; q < DB; ++q) Ls[q * 20 + lane] = PT[q];
+      }
+      __syncwarp();
+      float x[DB];
+#pragma unroll
+      for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+      for (int q = 0; q < DB - 1; ++q) {
+#pragma unroll
+        for (int i = q + 1; i < DB; ++i) x[i] = fmaf(-Ls[q * 20 + i], x[q], x[i]);
+      }
+      if (tv) {
+#pragma unroll
+        for (int i4 = 0; i4 < DB; i4 += 4)
+          *(float4*)&Li[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
+      }
+    }
+  };
+  // trailing update S[r, c] -= L21[r, :] U12[:, c] of panel jb for rows
+  // [jb+16, 128) and the columns [c0, c1) (multiples of 4), by `nth`
+  // threads numbered from `tid`
+  auto trailing = [&](int jb, int c0, int c1, int tid, int nth) {
+    const int nr = (LU_NB - jb - DB) / 4, ncl = (c1 - c0) / 4;
+    const float* Pb = S + jb * TLD + jb + DB;  // L21(r, q)
+    const float* Qb = S + c0 * TLD + jb;       // U12(q, c)
+    float* Cb = S + c0 * TLD + jb + DB;
+    for (int idx = tid; idx < nr * ncl; idx += nth) {
+      const int r0 = 4 * (idx % nr), cc = 4 * (idx / nr);
+      float acc[4][4] = {};
+      tile_mm<4>(Pb, Qb, r0, cc, 0, DB, acc);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float4 cv = *(float4*)&Cb[(cc + j) * TLD + r0];
+        cv.x -= acc[0][j]; cv.y -= acc[1][j]; cv.z -= acc[2][j]; cv.w -= acc[3][j];
+        *(float4*)&Cb[(cc + j) * TLD + r0] = cv;
+      }
+    }
+  };
+  // The phases are pipelined: after the block row of U of panel p, warps
+  // 0-3 update only panel p+1's columns, meet at a 128-thread named barrier
+  // and factor panel p+1 while warps 4-15 store panel p and apply the rest
+  // of its trailing update.  The 16 x 16 inverses are double-buffered by
+  // panel parity (panel p's are stored while panel p+1's are formed).
+  if (warp < 4) factor_panel(0, LiP);
+  __syncthreads();
+  for (int p = 0; p < LU_NB / DB; ++p) {
+    const int jb = p * DB;
+    float* Li = LiP + (p & 1) * 2 * DB * DB;
+    float* Ui = Li + DB * DB;
+    // ---- B: block row of U, U[p, >p] = Linv_pp A[p, >p]; Uinv_pp ----
     if (t < 128) {
-      const int c = jb + DB + t;  // U block row, one thread per column
+      const int c = jb + DB + t;  // one thread per column
       if (c < LU_NB) {
         float v[DB], o[DB];
 #pragma unroll
@@ -1012,7 +1040,7 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
         for (int q = 0; q < DB; ++q) {
 #pragma unroll
           for (int i4 = 0; i4 < DB; i4 += 4) {
-            const float4 l = *(const float4*)&LiP[q * DB + i4];
+            const float4 l = *(const float4*)&Li[q * DB + i4];
             o[i4] = fmaf(l.x, v[q], o[i4]);
             o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
             o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
@@ -1039,33 +1067,25 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
       if (lane < DB) {
 #pragma unroll
         for (int i4 = 0; i4 < DB; i4 += 4)
-          *(float4*)&UiP[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
+          *(float4*)&Ui[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
       }
     }
     __syncthreads();
-    // column block p of L\U and the two sub-block inverses are final
-    {
-      const int cs = jb + (t >> 5), r4 = 4 * (t & 31);
-      *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
-      SIk[p * 2 * DB * DB + t] = (t < DB * DB) ? LiP[t] : UiP[t - DB * DB];
-    }
-    // ---- C ----
-    if (jb + DB < LU_NB) {
-      const int n = LU_NB - jb - DB, nt = n / 4;
-      const float* Pb = S + jb * TLD + jb + DB;       // L21(r, q)
-      const float* Qb = S + (jb + DB) * TLD + jb;     // U12(q, c)
-      float* Cb = S + (jb + DB) * TLD + jb + DB;
-      for (int idx = t; idx < nt * nt; idx += 512) {
-        const int r0 = 4 * (idx % nt), c0 = 4 * (idx / nt);
-        float acc[4][4] = {};
-        tile_mm<4>(Pb, Qb, r0, c0, 0, DB, acc);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          float4 cv = *(float4*)&Cb[(c0 + j) * TLD + r0];
-          cv.x -= acc[0][j]; cv.y -= acc[1][j]; cv.z -= acc[2][j]; cv.w -= acc[3][j];
-          *(float4*)&Cb[(c0 + j) * TLD + r0] = cv;
-        }
+    if (warp < 4) {
+      if (p + 1 < LU_NB / DB) {
+        // ---- C1: the next panel's columns; then A of panel p+1 ----
+        trailing(jb, jb + DB, jb + 2 * DB, t, 128);
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        factor_panel(jb + DB, LiP + ((p + 1) & 1) * 2 * DB * DB);
       }
+    } else {
+      // ---- store column block p of L\U and its inverses; C2 ----
+      for (int idx = t - 128; idx < DB * 32; idx += 384) {
+        const int cs = jb + (idx >> 5), r4 = 4 * (idx & 31);
+        *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
+      }
+      for (int idx = t - 128; idx < 2 * DB * DB; idx += 384) SIk[p * 2 * DB * DB + idx] = Li[idx];
+      if (jb + 2 * DB < LU_NB) trailing(jb, jb + 2 * DB, LU_NB, t - 128, 384);
     }
     __syncthreads();
   }
