@@ -62,7 +62,9 @@ __global__ void __launch_bounds__(128) dibem_laplace_kernel(int nt, const double
   }
   __syncthreads();
   if (i0 >= nt) return;
-  const T inv2pi = T(1) / (T(2) * T(3.14159265358979323846));
+  // -log(R) / (2 pi k) with the constant's reciprocal formed once (per-entry
+  // FP64 divisions run on GB300's small FP64 pipe)
+  const T dcoef = T(1) / (T(2) * T(3.14159265358979323846) * kcond);
   const bool vec = (i0 + RPT <= nt) && ((ldf | ldd) % RPT == 0) && (((uintptr_t)F | (uintptr_t)D) % 16 == 0);
   for (int jj = 0; jj < nj; ++jj) {
     const int j = j0 + jj;
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(128) dibem_laplace_kernel(int nt, const double
         const T R2 = rx * rx + ry * ry;
         if (R2 > eps2) {
           const T R = sqrt(R2);
-          d[r] = -log(R) * inv2pi / kcond;
+          d[r] = -log(R) * dcoef;
           f[r] = dibem_phi<T>(kind, R, kcond, epsa);
         }
       }
@@ -122,7 +124,7 @@ __global__ void __launch_bounds__(128) dibem_kelvin_kernel(int nt, const double*
   if (i >= nt) return;
   const T pi = T(3.14159265358979323846);
   const T prod1 = T(4) * pi * (T(1) - nu);
-  const T base = T(2) * prod1 * mu;
+  const T inv_base = T(1) / (T(2) * prod1 * mu);
   for (int jj = 0; jj < nj; ++jj) {
     const int j = j0 + jj;
     T f = T(0), u11 = T(0), u12 = T(0), u22 = T(0);
@@ -133,11 +135,12 @@ __global__ void __launch_bounds__(128) dibem_kelvin_kernel(int nt, const double*
         const T R = sqrt(R2);
         f = dibem_phi<T>(kind, R, T(1), epsa);
         // U of the 2-D Kelvin solution (`_kelvin2d_UT`, Elasticity/Fundamental.jl)
-        const T dr1 = rx / R, dr2 = ry / R;
+        const T invR = T(1) / R;
+        const T dr1 = rx * invR, dr2 = ry * invR;
         const T prod2 = (T(3) - T(4) * nu) * (-log(R));
-        u11 = (prod2 + dr1 * dr1) / base;
-        u12 = (dr1 * dr2) / base;
-        u22 = (prod2 + dr2 * dr2) / base;
+        u11 = (prod2 + dr1 * dr1) * inv_base;
+        u12 = (dr1 * dr2) * inv_base;
+        u22 = (prod2 + dr2 * dr2) * inv_base;
       }
     }
     F[i + (size_t)j * ldf] = f;
