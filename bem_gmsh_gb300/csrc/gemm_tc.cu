@@ -20,8 +20,10 @@
 // measured alone on a 8064^2 update it beats the 32-wide 2-stage / 8-warp
 // single-CTA form by 12 % and the whole solve by 4 %.
 // The tensor core reads the top 19 bits of an FP32 operand (TF32), so the
-// FP32 matrix itself is the "hi" operand; the "lo" operands x - tf32(x) are
-// precomputed by k_split_lo.  Every mbarrier wait is bounded: on timeout
+// FP32 matrix itself is the "hi" operand; the "lo" operands x - tf32(x) and
+// the transposed L panel are written by the panel kernel of the look-ahead
+// LU (by k_split_lo in the plain blocked LU).  Every mbarrier wait is
+// bounded: on timeout
 // the CTA records an error, leaves the tile unwritten and frees its TMEM.
 #include <cuda.h>
 #include <cuda_runtime.h>
