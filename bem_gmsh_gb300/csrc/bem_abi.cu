@@ -13,6 +13,7 @@
 
 namespace bem {
 std::atomic<long long> g_launches{0};
+thread_local long long tl_launches = 0;
 thread_local KProf* tl_prof = nullptr;
 }  // namespace bem
 

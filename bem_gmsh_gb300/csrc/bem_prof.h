@@ -79,7 +79,12 @@ struct KProf {
 
 // process-wide count of kernel launches made by the library
 extern std::atomic<long long> g_launches;
-inline void count_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+// launches issued by this thread (a graph capture measures its own)
+extern thread_local long long tl_launches;
+inline void count_launches(long long k) {
+  g_launches.fetch_add(k, std::memory_order_relaxed);
+  tl_launches += k;
+}
 
 // profiler of the context whose C-ABI call is running on this thread
 extern thread_local KProf* tl_prof;

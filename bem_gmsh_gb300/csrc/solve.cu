@@ -176,7 +176,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   ++c->lu_graph_calls;
   int rc = 0;
   if (graphs && !c->lu_graph && c->lu_graph_calls >= 2) {
-    const long long l0 = bem::g_launches.load();
+    const long long l0 = bem::tl_launches;
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
@@ -192,8 +192,9 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       cudaGetLastError();
       rc = 0;
     }
-    c->lu_graph_launches = bem::g_launches.load() - l0;
+    c->lu_graph_launches = bem::tl_launches - l0;
     bem::g_launches.fetch_sub(c->lu_graph_launches);  // counted when replayed
+    bem::tl_launches = l0;
   }
   tf.start(st);
   if (graphs && c->lu_graph) {
