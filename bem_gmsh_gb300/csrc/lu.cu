@@ -668,12 +668,16 @@ __global__ void k_gemv64(const double* __restrict__ A, int64_t lda, int N,
 }
 
 // h[j] = sum_i V[i, j] w[i] for j < m  (V column-major, ld = N)
+// h[j] += V[:, j] . w over this CTA's slice of the rows (h zeroed before):
+// blockIdx.x = j, blockIdx.y = slice, so each vector is spread over
+// gridDim.y SMs (one SM's FP64 rate is a small fraction of the GPU's)
 __global__ void k_dots(const double* __restrict__ V, int64_t ldv, int N, int m,
                        const double* __restrict__ w, double* __restrict__ h) {
   const int j = blockIdx.x;
   if (j >= m) return;
   double acc = 0.0;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) acc = fma(V[i + (size_t)j * ldv], w[i], acc);
+  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < N; i += gridDim.y * blockDim.x)
+    acc = fma(V[i + (size_t)j * ldv], w[i], acc);
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ double s[32];
   if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
@@ -681,7 +685,7 @@ __global__ void k_dots(const double* __restrict__ V, int64_t ldv, int N, int m,
   if (threadIdx.x == 0) {
     double r = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) r += s[q];
-    h[j] = r;
+    atomicAdd(h + j, r);
   }
 }
 
@@ -1627,7 +1631,9 @@ void gemv64(const double* A, int64_t lda, int N, const double* x, double* y, cud
 
 void dots64(const double* V, int64_t ldv, int N, int m, const double* w, double* h, cudaStream_t st) {
   count_launches(1);
-  k_dots<<<m, 512, 0, st>>>(V, ldv, N, m, w, h);
+  cudaMemsetAsync(h, 0, sizeof(double) * m, st);
+  const int slices = (N + 2047) / 2048 < 16 ? (N + 2047) / 2048 : 16;
+  k_dots<<<dim3(m, slices > 0 ? slices : 1), 256, 0, st>>>(V, ldv, N, m, w, h);
 }
 void sub_vh64(const double* V, int64_t ldv, int N, int m, const double* h, double* w, cudaStream_t st) {
   count_launches(1);
