@@ -87,6 +87,8 @@ def load(build_if_missing: bool = False):
         "bem_selftest": ([ctx_p, ctypes.c_int, ctypes.c_int, PD], ctypes.c_int),
         "bem_kernel_times": ([ctx_p, PD, ctypes.POINTER(I64), ctypes.c_int], ctypes.c_int),
         "bem_launch_count": ([], I64),
+        "bem_dibem_ifid2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_int,
+                              VP, VP], ctypes.c_int),
         "bem_discretize2d": ([ctx_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, VP, VP, ctypes.c_int, VP, VP,
                               VP, VP, VP, VP, VP], ctypes.c_int),
         "bem_dibem_fd2d": ([ctx_p, ctypes.c_int, VP, VP, ctypes.c_int, D, D, ctypes.c_int, D, ctypes.c_int,

@@ -380,6 +380,24 @@ def adjoint_laplace(dad: BEMdata, q_target, npg: int = 16, near_factor: float = 
 RBF_KINDS = {"PHS1": 1, "PHS2": 2, "PHS3": 3, "PHS4": 4, "PHS5": 5, "PHS6": 6, "PHS7": 7, "fundamental": 10}
 
 
+def dibem_ifid(dad: BEMdata, rbf: str = "PHS3", dtype=np.float64, epsa: float = 1e-16, near_factor: float = 1.5,
+               ctx: _lib.Context | None = None):
+    """Far boundary sums IF, ID of the DIBEM domain integrals at every
+    collocation point (`_dibem_IFID_ka`, src/Laplace/DIBEM_GPU.jl:209-270);
+    near pairs are skipped for the caller's quadrature correction."""
+    ctx = ctx or _lib.default_context()
+    if not isinstance(dad.properties, Laplace):
+        raise ValueError("dibem_ifid supports Laplace meshes")
+    g, keep = geom_struct(dad)
+    IF = np.zeros(dad.nt, dtype=dtype)
+    ID = np.zeros(dad.nt, dtype=dtype)
+    dt = _lib.BEM_F64 if np.dtype(dtype) == np.float64 else _lib.BEM_F32
+    rc = ctx.L.bem_dibem_ifid2d(ctx.h, g, float(dad.properties.k), RBF_KINDS[rbf], float(epsa), float(near_factor),
+                                dt, _lib.BEM_MEM_HOST, _ptr(IF), _ptr(ID))
+    ctx.check(rc, "dibem_ifid")
+    return IF, ID
+
+
 def discretize(cad, p: int, ctx: _lib.Context | None = None):
     """Collocation nodes (ne, p+1, 2), outward normals, Jacobians (ne, p+1),
     element lengths (ne,) and Gauss weights (p+1,) of elements given by their

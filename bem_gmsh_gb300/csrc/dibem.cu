@@ -16,6 +16,7 @@
 #include <cmath>
 
 #include "bem_abi_internal.h"
+#include "bem_device.cuh"
 
 namespace bem {
 namespace {
@@ -153,10 +154,156 @@ __global__ void __launch_bounds__(128) dibem_kelvin_kernel(int nt, const double*
   }
 }
 
+// radial integral of each RBF kind (`_dibem_phi_int2d`, DIBEM_GPU.jl:141-171)
+template <typename T>
+__device__ __forceinline__ T dibem_phi_int(int kind, T R, T kcond, T epsa) {
+  const T R2 = R * R;
+  switch (kind) {
+    case 1: return (R2 * R) / T(3);
+    case 2: { const T R4 = R2 * R2; return (T(4) * R4 * log(R + epsa) - R4) / T(16); }
+    case 3: return (R2 * R2 * R) / T(5);
+    case 4: { const T R6 = R2 * R2 * R2; return R6 * log(R + epsa) / T(6) - R6 / T(36); }
+    case 5: return (R2 * R2 * R2 * R) / T(7);
+    case 6: { const T R8 = (R2 * R2) * (R2 * R2); return R8 * log(R + epsa) / T(8) - R8 / T(64); }
+    case 7: { const T R4 = R2 * R2; return (R4 * R4 * R) / T(9); }
+    default: return -(T(2) * R2 * log(R) - R2) / (T(8) * T(3.14159265358979323846) * kcond);
+  }
+}
+
+// Far boundary sums IF, ID of the DIBEM domain integrals (restating
+// `_dibem_IFID_kernel!`, DIBEM_GPU.jl:234-270): for every collocation point
+// i and boundary node j with R > 1e-10, unless the pair (i, element of j) is
+// near or i lies on that element (`_near_skip_mask`, the same exact FP64 test
+// as the assembly),
+//   IF_i += phi_int(R) w_j (r . n_j) / R^2,  ID_i += rad(R) w_j (r . n_j) / R^2,
+// rad(R) = -(2 R^2 log R - R^2) / (8 pi k) (`_dibem_rad_id2d`, :173-177),
+// w_j = Jacobian_j * elem_weight_k.  Grid: x over 128-point row blocks, y
+// over 32-element chunks staged in shared memory; partial sums are added
+// atomically.  A conservative FP64 box test skips the exact near test for
+// pairs that are far by a margin.
+constexpr int IF_EC = 32;
+struct IfidRule {
+  double ew[BEM_MAXNN];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) dibem_ifid_kernel(GeomDev g, IfidRule rw, int rbf, T kcond, T epsa,
+                                                        double nf, T* __restrict__ IF, T* __restrict__ ID) {
+  __shared__ double sx[IF_EC * BEM_MAXNN], sy[IF_EC * BEM_MAXNN];
+  __shared__ T snx[IF_EC * BEM_MAXNN], sny[IF_EC * BEM_MAXNN], sw[IF_EC * BEM_MAXNN];
+  __shared__ double blo[IF_EC][2], bhi[IF_EC][2], blim2[IF_EC], belen[IF_EC];
+  const int nn = g.nn;
+  const int e0 = blockIdx.y * IF_EC;
+  const int nel = min(IF_EC, g.ne - e0);
+  for (int idx = threadIdx.x; idx < nel * nn; idx += blockDim.x) {
+    const int j = e0 * nn + idx;
+    sx[idx] = g.px[j];
+    sy[idx] = g.py[j];
+    snx[idx] = (T)g.nx[j];
+    sny[idx] = (T)g.ny[j];
+    sw[idx] = (T)(g.jac[j] * rw.ew[idx % nn]);
+  }
+  for (int el = threadIdx.x; el < nel; el += blockDim.x) {
+    double lx = INFINITY, ly = INFINITY, hx = -INFINITY, hy = -INFINITY;
+    for (int q = 0; q < nn; ++q) {
+      const int j = (e0 + el) * nn + q;
+      lx = fmin(lx, g.px[j]);
+      ly = fmin(ly, g.py[j]);
+      hx = fmax(hx, g.px[j]);
+      hy = fmax(hy, g.py[j]);
+    }
+    blo[el][0] = lx; blo[el][1] = ly;
+    bhi[el][0] = hx; bhi[el][1] = hy;
+    const double L = g.elen[e0 + el];
+    belen[el] = L;
+    const double lim = nf * L;
+    blim2[el] = nf > 1e20 ? INFINITY : lim * lim * (1.0 + 1e-12);
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nt) return;
+  const V2 pf{g.px[i], g.py[i]};
+  const T pxi = (T)pf.x, pyi = (T)pf.y;
+  T aF = T(0), aD = T(0);
+  const T rmin = T(1e-10);
+  const T radc = T(1) / (T(8) * T(3.14159265358979323846) * kcond);
+  for (int el = 0; el < nel; ++el) {
+    const int e = e0 + el;
+    if (i >= e * nn && i < (e + 1) * nn) continue;  // source on the element
+    const double dx = fmax(fmax(blo[el][0] - pf.x, pf.x - bhi[el][0]), 0.0);
+    const double dy = fmax(fmax(blo[el][1] - pf.y, pf.y - bhi[el][1]), 0.0);
+    if (!(dx * dx + dy * dy > blim2[el])) {
+      V2 xg[BEM_MAXNN];
+      for (int q = 0; q < nn; ++q) xg[q] = V2{sx[el * nn + q], sy[el * nn + q]};
+      if (near_element(pf, xg, nn, belen[el], nf)) continue;
+    }
+    for (int q = 0; q < nn; ++q) {
+      const int s = el * nn + q;
+      const T rx = (T)sx[s] - pxi, ry = (T)sy[s] - pyi;
+      const T R2 = rx * rx + ry * ry;
+      const T R = sqrt(R2);
+      if (R > rmin) {
+        const T wJn = sw[s] * (rx * snx[s] + ry * sny[s]) / R2;
+        aF += dibem_phi_int<T>(rbf, R, kcond, epsa) * wJn;
+        aD += -(T(2) * R2 * log(R) - R2) * radc * wJn;
+      }
+    }
+  }
+  atomicAdd(IF + i, aF);
+  atomicAdd(ID + i, aD);
+}
+
 }  // namespace
 }  // namespace bem
 
 using namespace bem;
+
+extern "C" int bem_dibem_ifid2d(bem_ctx* c, const bem_geom2d* geom, double k, int rbf, double epsa,
+                                double near_factor, int dtype, int mem, void* IF, void* ID) {
+  if (!c || !geom || !IF || !ID) return BEM_ERR_INVALID;
+  if (!((rbf >= 1 && rbf <= 7) || rbf == 10)) return BEM_ERR_INVALID;
+  if (dtype != BEM_F32 && dtype != BEM_F64) return BEM_ERR_INVALID;
+  if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  if (!(k > 0) || !(near_factor >= 0)) return BEM_ERR_INVALID;
+  int rc = bem_check_geom(geom, 2, near_factor);
+  if (rc) return rc;
+  CallScope cs(c);
+  cudaSetDevice(c->device);
+  GeomDev gd;
+  Rules R;
+  rc = bem_stage_geom(c, geom, 2, mem, gd, R);
+  if (rc) return rc;
+  IfidRule rw{};
+  for (int q = 0; q < BEM_MAXNN; ++q) rw.ew[q] = R.ew[q];
+  const size_t esz = dtype == BEM_F32 ? 4 : 8;
+  const size_t nt = (size_t)gd.nt;
+  void *dF = IF, *dD = ID;
+  if (mem == BEM_MEM_HOST) {
+    void* o = c->get(bem_ctx::SLOT_OUT2, 2 * esz * nt);
+    if (!o) return BEM_ERR_NOMEM;
+    dF = o;
+    dD = (char*)o + esz * nt;
+  }
+  cudaMemsetAsync(dF, 0, esz * nt, c->stream);
+  cudaMemsetAsync(dD, 0, esz * nt, c->stream);
+  dim3 grid((unsigned)((nt + 127) / 128), (unsigned)((gd.ne + IF_EC - 1) / IF_EC));
+  if (dtype == BEM_F64)
+    dibem_ifid_kernel<double><<<grid, 128, 0, c->stream>>>(gd, rw, rbf, k, epsa, near_factor, (double*)dF,
+                                                            (double*)dD);
+  else
+    dibem_ifid_kernel<float><<<grid, 128, 0, c->stream>>>(gd, rw, rbf, (float)k, (float)epsa, near_factor,
+                                                           (float*)dF, (float*)dD);
+  count_launches(1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem_ifid_kernel");
+  if (mem == BEM_MEM_HOST) {
+    cudaMemcpyAsync(IF, dF, esz * nt, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(ID, dD, esz * nt, cudaMemcpyDeviceToHost, c->stream);
+  }
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem_ifid");
+  return BEM_OK;
+}
 
 extern "C" int bem_dibem_fd2d(bem_ctx* c, int nt, const double* px, const double* py, int kind, double prm0,
                               double prm1, int rbf, double epsa, int dtype, int mem, void* F, int64_t ldf,

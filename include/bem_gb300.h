@@ -234,6 +234,22 @@ int bem_dibem_fd2d(bem_ctx* ctx, int nt, const double* px, const double* py, int
                    int rbf, double epsa, int dtype, int mem, void* F, int64_t ldf, void* D, int64_t ldd);
 
 /*
+ * Far boundary sums of the DIBEM domain integrals over the collocation
+ * points of a 2-D Laplace mesh -- replaces `_dibem_IFID_ka` /
+ * `_dibem_IFID_kernel!` (src/Laplace/DIBEM_GPU.jl:209-270): for each point i,
+ *   IF_i = sum_j phi_int(R) w_j (r . n_j) / R^2,  ID_i = sum_j rad(R) w_j (r . n_j) / R^2
+ * over boundary nodes j with R = |x_j - x_i| > 1e-10, skipping the element
+ * of j when it is near x_i (near_factor, the assembly's exact test) or holds
+ * x_i (`_near_skip_mask`, src/Laplace/Assembly_GPU.jl:236-253); phi_int and
+ * rad are `_dibem_phi_int2d` / `_dibem_rad_id2d` (DIBEM_GPU.jl:141-177),
+ * w_j = Jacobian_j elem_weight_k.  The near-pair quadrature correction stays
+ * with the caller, as in the reference.  rbf as in bem_dibem_fd2d; dtype
+ * BEM_F32 / BEM_F64 the arithmetic and output type; IF, ID [nt].
+ */
+int bem_dibem_ifid2d(bem_ctx* ctx, const bem_geom2d* geom, double k, int rbf, double epsa, double near_factor,
+                     int dtype, int mem, void* IF, void* ID);
+
+/*
  * Boundary discretisation: ne elements, each given by ngeo equispaced CAD
  * nodes (cad_x/cad_y [ne*ngeo], element-major), to p+1 collocation nodes per
  * element at the Gauss-Legendre points with the Jacobian |dx/dxi|, the

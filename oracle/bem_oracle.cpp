@@ -1433,6 +1433,64 @@ void orc_dibem_fd2d(int nt, const double* px, const double* py, int kind, double
     }
 }
 
+// Radial integrals of the DIBEM boundary terms: phi_int of each RBF kind
+// (`_dibem_phi_int2d`, src/Laplace/DIBEM_GPU.jl:141-171) and of the Laplace
+// fundamental solution (`_dibem_rad_id2d`, :173-177).
+static double dibem_phi_int(int kind, double R, double k, double epsa) {
+  const double R2 = R * R;
+  switch (kind) {
+    case 1: return R2 * R / 3.0;
+    case 2: { const double R4 = R2 * R2; return (4.0 * R4 * std::log(R + epsa) - R4) / 16.0; }
+    case 3: return R2 * R2 * R / 5.0;
+    case 4: { const double R6 = R2 * R2 * R2; return R6 * std::log(R + epsa) / 6.0 - R6 / 36.0; }
+    case 5: return R2 * R2 * R2 * R / 7.0;
+    case 6: { const double R8 = (R2 * R2) * (R2 * R2); return R8 * std::log(R + epsa) / 8.0 - R8 / 64.0; }
+    case 7: { const double R4 = R2 * R2; return R4 * R4 * R / 9.0; }
+    default: return -(2.0 * R2 * std::log(R) - R2) / (8.0 * kPi * k);
+  }
+}
+static double dibem_rad_id(double R, double k) {
+  const double R2 = R * R;
+  return -(2.0 * R2 * std::log(R) - R2) / (8.0 * kPi * k);
+}
+
+// Far (lumped) boundary sums of the DIBEM domain integrals, restating
+// `_dibem_IFID_kernel!` (src/Laplace/DIBEM_GPU.jl:234-270): for every
+// collocation point i and boundary node j with R = |x_j - x_i| > 1e-10, and
+// the element e of node j unless (i, e) is near or i lies on e (the mask of
+// `_near_skip_mask`, src/Laplace/Assembly_GPU.jl:236-253):
+//   IF_i += phi_int(R) w_j (r . n_j) / R^2,   ID_i += rad(R) w_j (r . n_j) / R^2
+// with w_j = Jacobian_j * elem_weight_k (discontinuous elements: one element
+// per node).
+int orc_dibem_ifid2d(const OrcGeom* og, double k, int rbf, double epsa, double near_factor, double* IF,
+                     double* ID) {
+  Geom g = to_geom(og);
+  const int nn = g.p + 1;
+  for (int i = 0; i < g.nt; ++i) {
+    const V2 pf{g.px[i], g.py[i]};
+    double aF = 0.0, aD = 0.0;
+    for (int e = 0; e < g.ne; ++e) {
+      V2 xg[16];
+      for (int q = 0; q < nn; ++q) xg[q] = V2{g.px[e * nn + q], g.py[e * nn + q]};
+      const bool on = (i >= e * nn && i < (e + 1) * nn);
+      if (on || near_element(pf, xg, nn, g.elen[e], near_factor)) continue;
+      for (int q = 0; q < nn; ++q) {
+        const int j = e * nn + q;
+        const double rx = g.px[j] - pf.x, ry = g.py[j] - pf.y;
+        const double R2 = rx * rx + ry * ry;
+        const double R = std::sqrt(R2);
+        if (!(R > 1e-10)) continue;
+        const double wJn = g.jac[j] * g.ew[q] * (rx * g.nx[j] + ry * g.ny[j]) / R2;
+        aF += dibem_phi_int(rbf, R, k, epsa) * wJn;
+        aD += dibem_rad_id(R, k) * wJn;
+      }
+    }
+    IF[i] = aF;
+    ID[i] = aD;
+  }
+  return 0;
+}
+
 // interior_laplace (src/Laplace/Lubrication.jl:399-416): potential at m
 // interior points, every element through integrate_element.
 int orc_interior_laplace(const OrcGeom* og, double k, int npg, int nearfield, const double* T,

@@ -77,6 +77,8 @@ def lib():
         _lib.orc_interior_laplace.argtypes = [ctypes.POINTER(OrcGeom), d, i, i, P, P, i, P, P, P]
         _lib.orc_interior_laplace.restype = i
         _lib.orc_dibem_fd2d.argtypes = [i, P, P, i, d, d, i, d, P, P]
+        _lib.orc_dibem_ifid2d.argtypes = [ctypes.POINTER(OrcGeom), d, i, d, d, P, P]
+        _lib.orc_dibem_ifid2d.restype = i
     return _lib
 
 
@@ -199,6 +201,18 @@ def dibem_fd(pts, kind=0, prm0=1.0, prm1=0.0, rbf=3, epsa=1e-16):
     D = np.zeros((dof * nt, dof * nt), order="F")
     lib().orc_dibem_fd2d(nt, _p(px), _p(py), kind, float(prm0), float(prm1), int(rbf), float(epsa), _p(F), _p(D))
     return F, D
+
+
+def dibem_ifid(dad, rbf=3, epsa=1e-16, near_factor=1.5):
+    """Far boundary sums IF, ID of the DIBEM domain integrals
+    (`_dibem_IFID_kernel!`, src/Laplace/DIBEM_GPU.jl:234-270)."""
+    L = lib()
+    g, keep = make_geom(dad)
+    IF = np.zeros(dad.nt)
+    ID = np.zeros(dad.nt)
+    L.orc_dibem_ifid2d(ctypes.byref(g), float(dad.properties.k), int(rbf), float(epsa), float(near_factor),
+                       _p(IF), _p(ID))
+    return IF, ID
 
 
 def discretize(cad, p):

@@ -35,3 +35,31 @@ def test_large_star_fp32():
     F, D = dibem_fd(dad, rbf="PHS3", dtype=np.float32)
     assert F.shape == (3000, 3000) and np.isfinite(F).all() and np.isfinite(D).all()
     np.testing.assert_allclose(F, F.T, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("rbf", ["PHS1", "PHS3", "PHS6", "fundamental"])
+def test_ifid_matches_oracle(orc, rbf):
+    from bem_gmsh_gb300.api import RBF_KINDS, dibem_ifid
+    dad = star_domain(400, p=2, seed=3, pontointerno=True)
+    IF, ID = dibem_ifid(dad, rbf=rbf)
+    IFr, IDr = orc.dibem_ifid(dad, rbf=RBF_KINDS[rbf])
+    assert np.max(np.abs(IF - IFr)) <= 1e-12 * np.max(np.abs(IFr))
+    assert np.max(np.abs(ID - IDr)) <= 1e-12 * np.max(np.abs(IDr))
+    IF32, ID32 = dibem_ifid(dad, rbf=rbf, dtype=np.float32)
+    assert np.max(np.abs(IF32 - IFr)) <= 1e-4 * np.max(np.abs(IFr))
+    assert np.max(np.abs(ID32 - IDr)) <= 1e-4 * np.max(np.abs(IDr))
+
+
+def test_ifid_radial_integration_identity_on_device():
+    """At the centre of the unit disc IF -> 2 pi / 5 (PHS3) and ID -> 1 / 4."""
+    from bem_gmsh_gb300.api import dibem_ifid
+    from bem_gmsh_gb300.geometry import from_cad
+    from bem_gmsh_gb300 import Laplace
+    ne = 512
+    th = 2 * np.pi * (np.arange(ne)[:, None] + np.arange(3)[None, :] / 2) / ne
+    cad = np.stack([np.cos(th), np.sin(th)], -1)
+    dad = from_cad("circle", cad, 2, Laplace(1.0), np.ones((ne, 1), np.int32), np.zeros((ne, 1)),
+                   internal=[[0.0, 0.0]])
+    IF, ID = dibem_ifid(dad, rbf="PHS3")
+    assert IF[-1] == pytest.approx(2 * np.pi / 5, rel=1e-9)
+    assert ID[-1] == pytest.approx(0.25, rel=1e-12)
