@@ -212,6 +212,16 @@ def extra_configs(ctx):
                      "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / hbm_gbs}
         del Fb, Db
     ctx.set_stream(0)
+    # DIBEM far boundary sums IF, ID at the C2 points (nt x n pairs)
+    from bem_gmsh_gb300.api import dibem_ifid
+    for name, tdt in (("ifid_fp32", np.float32), ("ifid_fp64", np.float64)):
+        dibem_ifid(d2, rbf="PHS3", dtype=tdt, ctx=ctx)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            dibem_ifid(d2, rbf="PHS3", dtype=tdt, ctx=ctx)
+        ms = (time.perf_counter() - t0) / 5 * 1e3
+        dib[name] = {"ms": ms, "pairs_per_s": float(nt) * d2.n / (ms * 1e-3),
+                     "note": "wall clock per call through the API with host buffers"}
     out["dibem_fd_c2"] = {"N": nt, "rbf": "PHS3", **dib,
                           "note": "F and D (2 N^2 entries) written to device buffers; CUDA events on the "
                                   "launching stream around each call (one launch, plus its launch latency)"}
