@@ -356,9 +356,18 @@ extern "C" int bem_adjoint_laplace2d(bem_ctx* c, const bem_geom2d* g, double k, 
   const int prec = (c->opt_far_df >= 1) ? 3 : 1;
   rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, prec, A, ld, nullptr, b);
   if (rc) return rc;
-  // device copies of BC, BV (staged by the assembly for host inputs)
-  const int32_t* dBC = mem == BEM_MEM_HOST ? (const int32_t*)c->get(bem_ctx::SLOT_BC, sizeof(int32_t) * N) : BC;
-  const double* dBV = mem == BEM_MEM_HOST ? (const double*)c->get(bem_ctx::SLOT_BV, sizeof(double) * N) : BV;
+  // device copies of BC, BV for the split of the forward solution
+  const int32_t* dBC = BC;
+  const double* dBV = BV;
+  if (mem == BEM_MEM_HOST) {
+    int32_t* hbc = (int32_t*)c->get(bem_ctx::SLOT_BC, sizeof(int32_t) * (size_t)n);
+    double* hbv = (double*)c->get(bem_ctx::SLOT_BV, sizeof(double) * (size_t)n);
+    if (!hbc || !hbv) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(hbc, BC, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(hbv, BV, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    dBC = hbc;
+    dBV = hbv;
+  }
   bem_solve_stats st{};
   rc = bem_solve_mixed_dev(c, N, A, ld, b, tol, max_iter, 1, u, &st);
   if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;

@@ -151,6 +151,50 @@ void* bem_ctx::get(int slot, size_t bytes) {
   return b.p;
 }
 
+void bem_ctx::pin_issued() {
+  if (!pin_ev && cudaEventCreateWithFlags(&pin_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    pin_ev = nullptr;
+  }
+  if (pin_ev) {
+    cudaEventRecord(pin_ev, stream);
+    pin_pending = true;
+  } else {
+    cudaStreamSynchronize(stream);
+  }
+}
+
+char* bem_ctx::pinned(size_t bytes) {
+  if (pin_pending) {
+    cudaEventSynchronize(pin_ev);
+    pin_pending = false;
+  }
+  if (bytes == 0) bytes = 64;
+  if (pin_bytes >= bytes) return pin;
+  if (pin) {
+    cudaStreamSynchronize(stream);
+    cudaFreeHost(pin);
+  }
+  pin = nullptr;
+  pin_bytes = 0;
+  size_t want = (bytes + bytes / 8 + 4095) / 4096 * 4096;
+  if (cudaHostAlloc((void**)&pin, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    pin = nullptr;
+    return nullptr;
+  }
+  pin_bytes = want;
+  return pin;
+}
+
+cudaEvent_t bem_ctx::timing_event(int i) {
+  if (!tev[i] && cudaEventCreate(&tev[i]) != cudaSuccess) {
+    cudaGetLastError();
+    tev[i] = nullptr;
+  }
+  return tev[i];
+}
+
 bool bem_ctx::lookahead_ready(int k) {
   if (!la_stream) {
     int lo = 0, hi = 0;
@@ -211,6 +255,10 @@ extern "C" int bem_ctx_destroy(bem_ctx* c) {
   bem_release_solver(c);
   for (auto& b : c->slots)
     if (b.p) cudaFree(b.p);
+  if (c->pin) cudaFreeHost(c->pin);
+  if (c->pin_ev) cudaEventDestroy(c->pin_ev);
+  for (auto e : c->tev)
+    if (e) cudaEventDestroy(e);
   c->prof.release();
   for (auto e : c->events) cudaEventDestroy(e);
   if (c->asm_fork) cudaEventDestroy(c->asm_fork);
@@ -266,7 +314,8 @@ int bem_check_geom(const bem_geom2d* g, int npg, double near_factor) {
   return BEM_OK;
 }
 
-int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& gd, Rules& R) {
+int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& gd, Rules& R, int64_t nb,
+                   const int32_t* BC, const double* BV, const int32_t** dBC, const double** dBV) {
   const int nn = g->p + 1;
   double ew[BEM_MAXNN];
   if (mem == BEM_MEM_HOST) {
@@ -284,16 +333,25 @@ int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& g
   if (mem == BEM_MEM_DEVICE) {
     gd.px = g->px; gd.py = g->py; gd.nx = g->nx; gd.ny = g->ny;
     gd.jac = g->jac; gd.elen = g->elen; gd.gx = g->geo_x; gd.gy = g->geo_y;
+    if (dBC) *dBC = BC;
+    if (dBV) *dBV = BV;
     return BEM_OK;
   }
+  // one device block [geometry | BV | BC], filled from the same layout in
+  // the pinned buffer by one copy
+  const bool bcs = nb > 0 && BC && BV && dBC && dBV;
   const size_t ng = (size_t)g->ne * g->ngeo;
   const size_t tot = 2 * (size_t)g->nt + 3 * (size_t)g->n + (size_t)g->ne + 2 * ng;
-  double* d = (double*)c->get(bem_ctx::SLOT_GEOM, tot * sizeof(double));
-  if (!d) return BEM_ERR_NOMEM;
+  const size_t nbv = bcs ? (size_t)nb : 0;
+  const size_t nbc = bcs ? ((size_t)nb + 1) / 2 : 0;  // int32 codes, in doubles
+  const size_t words = tot + nbv + nbc;
+  double* d = (double*)c->get(bem_ctx::SLOT_GEOM, words * sizeof(double));
+  double* h = (double*)c->pinned(words * sizeof(double));
+  if (!d || !h) return BEM_ERR_NOMEM;
   size_t o = 0;
   auto put = [&](const double* src, size_t cnt) -> const double* {
-    double* dst = d + o;
-    if (cnt) cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (cnt) std::memcpy(h + o, src, cnt * sizeof(double));
+    const double* dst = d + o;
     o += cnt;
     return dst;
   };
@@ -305,6 +363,14 @@ int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& g
   gd.elen = put(g->elen, g->ne);
   gd.gx = ng ? put(g->geo_x, ng) : nullptr;
   gd.gy = ng ? put(g->geo_y, ng) : nullptr;
+  if (bcs) {
+    *dBV = put(BV, nbv);
+    std::memcpy(h + o, BC, sizeof(int32_t) * (size_t)nb);
+    *dBC = (const int32_t*)(d + o);
+    o += nbc;
+  }
+  cudaMemcpyAsync(d, h, o * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  c->pin_issued();
   return BEM_OK;
 }
 
@@ -443,24 +509,12 @@ int bem_assemble_system_dev(bem_ctx* c, const bem_geom2d* g, const Physics& ph, 
   const int64_t nb = (int64_t)dof * g->n;
   cudaSetDevice(c->device);
   AsmRequest q{};
-  rc = bem_stage_geom(c, g, npg, mem, q.g, q.R);
+  rc = bem_stage_geom(c, g, npg, mem, q.g, q.R, nb, BC, BV, &q.bc, &q.bv);
   if (rc) return rc;
   q.ph = ph;
   q.near_factor = nf;
   q.prec = prec;
   q.fused = 1;
-  if (mem == BEM_MEM_HOST) {
-    int32_t* dbc = (int32_t*)c->get(bem_ctx::SLOT_BC, sizeof(int32_t) * (size_t)nb);
-    double* dbv = (double*)c->get(bem_ctx::SLOT_BV, sizeof(double) * (size_t)nb);
-    if (!dbc || !dbv) return BEM_ERR_NOMEM;
-    cudaMemcpyAsync(dbc, BC, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(dbv, BV, sizeof(double) * nb, cudaMemcpyHostToDevice, c->stream);
-    q.bc = dbc;
-    q.bv = dbv;
-  } else {
-    q.bc = BC;
-    q.bv = BV;
-  }
   q.H = A;
   q.ld = lda;
   q.G = nullptr;

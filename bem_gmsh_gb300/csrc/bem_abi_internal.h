@@ -57,6 +57,21 @@ struct bem_ctx {
 
   // Grow-only device buffer for `slot` (NULL on allocation failure).
   void* get(int slot, size_t bytes);
+  // Grow-only page-locked host staging buffer: a call's inputs go up and its
+  // small results come back through it, one asynchronous copy each.  Growing
+  // synchronizes the context's stream first (no copy from the old buffer is
+  // in flight when it is freed).  NULL on allocation failure.
+  char* pinned(size_t bytes);
+  // marks the end of the last copy issued from the pinned buffer; pinned()
+  // waits for it before handing the buffer out again
+  void pin_issued();
+  char* pin = nullptr;
+  size_t pin_bytes = 0;
+  cudaEvent_t pin_ev = nullptr;
+  bool pin_pending = false;
+  // timing events of the solve stages (created on first use)
+  cudaEvent_t timing_event(int i);
+  cudaEvent_t tev[6] = {};
   int cuda_fail(cudaError_t e, const char* where);
 };
 
@@ -79,8 +94,12 @@ int bem_check_geom(const bem_geom2d* g, int npg, double near_factor);
 void bem_release_solver(bem_ctx* c);
 // host-side rule tables of an assembly (element Gauss weights on the host)
 void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, bem::Rules& R);
+// Stages the geometry on the device (host inputs: one copy through the
+// pinned buffer, together with the nb boundary-condition codes and values
+// when BC/BV are given; device inputs are used in place).
 int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, bem::GeomDev& gd,
-                   bem::Rules& R);
+                   bem::Rules& R, int64_t nb = 0, const int32_t* BC = nullptr, const double* BV = nullptr,
+                   const int32_t** dBC = nullptr, const double** dBV = nullptr);
 int bem_run_assembly(bem_ctx* c, bem::AsmRequest& q);
 int bem_assemble_system_dev(bem_ctx* c, const bem_geom2d* g, const bem::Physics& ph,
                             const int32_t* BC, const double* BV, int npg, double nf, int mem,

@@ -65,11 +65,23 @@ Cusolver* cusolver() {
 
 struct Timer {
   cudaEvent_t a = nullptr, b = nullptr;
+  bool own = true;
   Timer() {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
   }
+  // borrows the context's timing events 2i, 2i+1 (no create/destroy per call)
+  Timer(bem_ctx* c, int i) {
+    a = c->timing_event(2 * i);
+    b = c->timing_event(2 * i + 1);
+    own = !a || !b;
+    if (own) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+    }
+  }
   ~Timer() {
+    if (!own) return;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
   }
@@ -83,12 +95,31 @@ struct Timer {
   }
 };
 
-double dev_dot(bem_ctx* c, const double* v, const double* w, int N, double* hbuf) {
+// <v, w> on the device, read back through the pinned word `hpin`
+double dev_dot(bem_ctx* c, const double* v, const double* w, int N, double* hbuf, double* hpin) {
   bem::dots64(v, N, N, 1, w, hbuf, c->stream);
-  double h = 0.0;
-  cudaMemcpyAsync(&h, hbuf, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(hpin, hbuf, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   cudaStreamSynchronize(c->stream);
-  return h;
+  return *hpin;
+}
+
+// Pinned host words of one solve: the Gram-Schmidt coefficients (64), the
+// least-squares solution (32), a dot product, the LU status words.
+struct SolvePin {
+  double* hh;
+  double* y;
+  double* dot;
+  int* info;  // 4 ints
+};
+bool solve_pin(bem_ctx* c, SolvePin& p) {
+  char* b = c->pinned(1024);
+  if (!b) return false;
+  double* d = (double*)b;
+  p.hh = d;
+  p.y = d + 64;
+  p.dot = d + 96;
+  p.info = (int*)(d + 100);
+  return true;
 }
 
 }  // namespace
@@ -129,7 +160,9 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   cudaMemsetAsync(tags, 0, sizeof(unsigned long long) * 2 * (size_t)Npad, c->stream);
   int epoch = 0;
   int* werr = info + 1;
-  Timer tf, tr;
+  SolvePin pin;
+  if (!solve_pin(c, pin)) return BEM_ERR_NOMEM;
+  Timer tf(c, 1), tr(c, 2);
   bem::TcPlan tcp[2];
   const bool use_tc = c->opt_tcgen05 && x3 && c->lookahead_ready(K);
   if (use_tc) {
@@ -206,7 +239,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   }
   if (rc) return c->cuda_fail((cudaError_t)rc, "lu_factor");
   tf.stop(st);
-  int hinfo2[2] = {0, 0};
+  int* hinfo2 = pin.info;
   cudaMemcpyAsync(hinfo2, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return c->cuda_fail(e, "factor");
@@ -230,7 +263,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   };
   tr.start(st);
   cudaMemsetAsync(x, 0, sizeof(double) * N, st);
-  const double bnorm = std::sqrt(dev_dot(c, b, b, N, hbuf));
+  const double bnorm = std::sqrt(dev_dot(c, b, b, N, hbuf, pin.dot));
   if (!(bnorm > 0)) {
     tr.stop(st);
     if (stats) { stats->iterations = 0; stats->rel_residual = 0; stats->status = BEM_OK; stats->t_refine_ms = tr.ms(); }
@@ -249,7 +282,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
     else
       bem::residual64(A64, lda, N, x, b, w, st);
     x_zero = false;
-    double beta = std::sqrt(dev_dot(c, w, w, N, hbuf));
+    double beta = std::sqrt(dev_dot(c, w, w, N, hbuf, pin.dot));
     relres = beta / bnorm;
     if (relres <= tol) { converged = true; break; }
     // stagnation at the FP64 rounding floor (a tol below eps |A| |x| / |b|
@@ -275,8 +308,8 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       }
       bem::dots64(w, N, N, 1, w, hbuf + 62, st);
       bem::scale_by_norm64(w, hbuf + 62, V + (size_t)(j + 1) * N, N, st);
-      double hh[64];
-      cudaMemcpyAsync(hh, hbuf, sizeof(double) * 64, cudaMemcpyDeviceToHost, st);
+      const double* hh = pin.hh;
+      cudaMemcpyAsync(pin.hh, hbuf, sizeof(double) * 64, cudaMemcpyDeviceToHost, st);
       cudaStreamSynchronize(st);
       std::vector<double> h(j + 2, 0.0);
       for (int q = 0; q <= j; ++q) h[q] = hh[q] + hh[32 + q];
@@ -304,20 +337,21 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       for (int p = q + 1; p < j; ++p) s -= H[q + (size_t)p * (m + 1)] * y[p];
       y[q] = s / H[q + (size_t)q * (m + 1)];
     }
-    cudaMemcpyAsync(hbuf, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, st);
+    std::memcpy(pin.y, y.data(), sizeof(double) * j);
+    cudaMemcpyAsync(hbuf, pin.y, sizeof(double) * j, cudaMemcpyHostToDevice, st);
     bem::add_zy64(Z, N, N, j, hbuf, x, st);
   }
   if (!converged) {
     bem::residual64(A64, lda, N, x, b, w, st);
-    relres = std::sqrt(dev_dot(c, w, w, N, hbuf)) / bnorm;
+    relres = std::sqrt(dev_dot(c, w, w, N, hbuf, pin.dot)) / bnorm;
     converged = relres <= tol;
   }
   tr.stop(st);
+  cudaMemcpyAsync(pin.info + 2, werr, sizeof(int), cudaMemcpyDeviceToHost, st);
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return c->cuda_fail(e, "refinement");
   if (prc) return c->cuda_fail((cudaError_t)prc, "triangular solve launch");
-  int herr = 0;
-  cudaMemcpy(&herr, werr, sizeof(int), cudaMemcpyDeviceToHost);
+  const int herr = pin.info[2];
   if (herr) {
     c->last_error = "triangular-solve wait timed out";
     return BEM_ERR_INTERNAL;
@@ -355,7 +389,9 @@ int bem_solve_fp64_dev(bem_ctx* c, int N, double* A64, int64_t lda, const double
   int* ipiv = (int*)c->get(bem_ctx::SLOT_LU4, sizeof(int) * ((size_t)N + 16));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
   if (!work || !ipiv || !info) return BEM_ERR_NOMEM;
-  Timer tf, tr;
+  SolvePin pin;
+  if (!solve_pin(c, pin)) return BEM_ERR_NOMEM;
+  Timer tf(c, 1), tr(c, 2);
   tf.start(st);
   if (cs->getrf(c->cusolver_handle, N, N, A64, (int)lda, work, ipiv, info) != 0) return BEM_ERR_CUDA;
   tf.stop(st);
@@ -363,8 +399,8 @@ int bem_solve_fp64_dev(bem_ctx* c, int N, double* A64, int64_t lda, const double
   cudaMemcpyAsync(x, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, st);
   if (cs->getrs(c->cusolver_handle, 0, N, 1, A64, (int)lda, ipiv, x, N, info + 1) != 0) return BEM_ERR_CUDA;
   tr.stop(st);
-  int hi[2] = {0, 0};
-  cudaMemcpyAsync(hi, info, sizeof(hi), cudaMemcpyDeviceToHost, st);
+  const int* hi = pin.info;
+  cudaMemcpyAsync(pin.info, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return c->cuda_fail(e, "cuSOLVER getrf/getrs");
   if (stats) {
@@ -457,7 +493,7 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   if (!A || !bx) return BEM_ERR_NOMEM;
   double* b = bx;
   double* dx = mem == BEM_MEM_DEVICE ? x : bx + N;
-  Timer ta;
+  Timer ta(c, 0);
   ta.start(c->stream);
   // the FP64 comparison path keeps FP64 arithmetic throughout
   const int prec = (mode == BEM_SOLVE_MIXED && kind == 0 && c->opt_far_df >= 1) ? 3 : 1;
@@ -470,9 +506,12 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   if (stats) stats->t_assemble_ms = t_asm;
   if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;
   if (mem == BEM_MEM_HOST) {
-    cudaMemcpyAsync(x, dx, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
+    double* hx = (double*)c->pinned(sizeof(double) * (size_t)N);
+    if (!hx) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(hx, dx, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "copy x to host");
+    std::memcpy(x, hx, sizeof(double) * N);
   }
   return rc;
 }
