@@ -293,17 +293,68 @@ def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib
     return out
 
 
+# worker counts chosen by tune_batch, per batch shape
+_BATCH_TUNED: dict = {}
+BATCH_WORKERS_DEFAULT = 16
+
+
+def _batch_key(dads, npg: int, mode: str):
+    """Shape class of a batch: mode, rule, and the number of domains and
+    sum of N^2 each to within a factor of two."""
+    nt = np.fromiter((d.nt * d.ndof for d in dads), dtype=np.float64, count=len(dads))
+    return (mode, int(npg), len(dads).bit_length(), int(np.sum(nt * nt)).bit_length())
+
+
+def batch_workers(dads, npg: int = 20, mode: str = "mixed") -> int:
+    """Worker count `solve_batch(..., nworkers=0)` uses for this batch: the
+    tuned one for its shape class, else BATCH_WORKERS_DEFAULT."""
+    return _BATCH_TUNED.get(_batch_key(list(dads), npg, mode), BATCH_WORKERS_DEFAULT)
+
+
+def tune_batch(dads, npg: int = 20, mode: str = "mixed", candidates=(4, 8, 16, 24, 32),
+               ctx: _lib.Context | None = None, repeats: int = 1, **kw):
+    """Autotuner of the batched solve's concurrency (the number of worker
+    streams that overlap the domains' pipelines).
+
+    Runs one warm-up pass at the largest candidate (it sizes every worker's
+    device workspace and page-locked staging), then times `solve_batch` over
+    `dads` `repeats` times per candidate and keeps the fastest (minimum over
+    repeats) for batches of this shape class (`_batch_key`); later
+    `solve_batch(..., nworkers=0)` calls use it.  The solutions do not depend
+    on the worker count.  Returns (best, {count: seconds})."""
+    import time
+    dads = list(dads)
+    cands = sorted({int(c) for c in candidates if 1 <= int(c) <= 32})
+    if not dads or not cands:
+        raise ValueError("tune_batch: needs domains and worker counts in 1..32")
+    solve_batch(dads, npg=npg, mode=mode, nworkers=cands[-1], ctx=ctx, **kw)
+    times = {}
+    for w in cands:
+        best = float("inf")
+        for _ in range(max(1, int(repeats))):
+            t0 = time.perf_counter()
+            solve_batch(dads, npg=npg, mode=mode, nworkers=w, ctx=ctx, **kw)
+            best = min(best, time.perf_counter() - t0)
+        times[w] = best
+    pick = min(times, key=lambda w: (times[w], w))
+    _BATCH_TUNED[_batch_key(dads, npg, mode)] = pick
+    return pick, times
+
+
 def solve_batch(dads, npg: int = 20, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 200,
-                near_factor: float = 1.5, nworkers: int = 8, ctx: _lib.Context | None = None,
+                near_factor: float = 1.5, nworkers: int = 0, ctx: _lib.Context | None = None,
                 return_stats: bool = False):
     """`solve(dad)` for many independent domains in one call
     (bem_solve2d_batch): every domain is assembled and solved on the GPU;
-    worker threads with their own streams overlap the domains.  All domains
-    share the physics of the first one.  Returns the list of solution
-    vectors (and the per-domain stats)."""
+    worker threads with their own streams overlap the domains (`nworkers`;
+    0: the count `tune_batch` chose for this batch shape, else
+    BATCH_WORKERS_DEFAULT).  All domains share the physics of the first one.
+    Returns the list of solution vectors (and the per-domain stats)."""
     dads = list(dads)
     if not dads:
         return ([], []) if return_stats else []
+    if nworkers == 0:
+        nworkers = batch_workers(dads, npg, mode)
     ctx = ctx or _lib.default_context()
     pr = dads[0].properties
     kind = 0 if isinstance(pr, Laplace) else 1

@@ -31,6 +31,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# the batched solve drives up to 32 worker streams, each with side streams:
+# 32 hardware work queues instead of the default 8 keep them from sharing
+# queues (set before the first CUDA call of the process)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = ("solves/sec & H+G entries/sec at N=8192, mixed vs FP64 GPU, "
           "≤1e-10 rel err vs FP64")
@@ -142,15 +146,16 @@ def extra_configs(ctx):
     public API with host buffers."""
     import numpy as np
     from bem_gmsh_gb300.geometry import c4_node_counts, c4_domains, star_adjoint_case
-    from bem_gmsh_gb300.api import solve_batch, adjoint_laplace, solve
+    from bem_gmsh_gb300.api import solve_batch, adjoint_laplace, solve, tune_batch
     out = {}
     sizes = c4_node_counts(512, seed=0)
     dads = c4_domains(sizes)
-    # warm-up: one full pass sizes every worker's workspace for its largest
-    # domain, so that the timed pass allocates nothing
-    solve_batch(dads, npg=16, mode="mixed", nworkers=16, ctx=ctx)
+    # warm-up: the autotuner's passes (one at 32 workers, then one per
+    # candidate count) size every worker's workspace, so that the timed pass
+    # allocates nothing, and choose the worker count it runs with
+    workers, tuning = tune_batch(dads, npg=16, mode="mixed", candidates=(8, 16, 24, 32), ctx=ctx)
     t = time.perf_counter()
-    xs, st = solve_batch(dads, npg=16, mode="mixed", nworkers=16, ctx=ctx, return_stats=True)
+    xs, st = solve_batch(dads, npg=16, mode="mixed", nworkers=0, ctx=ctx, return_stats=True)
     dt = time.perf_counter() - t
     ent = float(np.sum(sizes.astype(float) ** 2))
     idx = np.linspace(0, len(dads) - 1, 64).astype(int)
@@ -162,11 +167,12 @@ def extra_configs(ctx):
     out["batched_c4"] = {
         "domains": len(dads), "nodes_min": int(sizes.min()), "nodes_max": int(sizes.max()),
         "sum_entries": ent, "seconds": dt, "solves_per_s": len(dads) / dt, "entries_per_s": ent / dt,
-        "workers": 16, "max_gmres_iterations": int(max(s["iterations"] for s in st)),
+        "workers": workers, "tuning_s": {str(k): round(v, 4) for k, v in tuning.items()},
+        "max_gmres_iterations": int(max(s["iterations"] for s in st)),
         "fp64_sample": {"domains": len(idx), "seconds": dt64, "max_rel_err": max(errs),
                         "median_rel_err": float(np.median(errs))},
-        "note": "wall clock through solve_batch with host buffers, after one warm-up pass; per-domain "
-                "pipelines on 16 worker streams"}
+        "note": "wall clock through solve_batch with host buffers, after the autotuner's passes; "
+                "per-domain pipelines on the tuned number of worker streams"}
     cases = [star_adjoint_case(341, p=2, seed=s) for s in range(64)]
     qts = []
     for d, tg in cases:

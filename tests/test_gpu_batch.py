@@ -35,3 +35,17 @@ def test_batch_invalid_arguments():
     rc = ctx.L.bem_solve2d_batch(ctx.h, 1, None, 0, 1.0, 0.0, None, None, None, 16, 1.5, 1, 1e-14, 100,
                                  0, None, None, 4, None)
     assert rc == 1
+
+
+def test_tune_batch_picks_a_candidate_and_keeps_results():
+    from bem_gmsh_gb300 import api
+    sizes = c4_sizes(12, hi=900, seed=5)
+    dads = make_batch(sizes)
+    best, times = api.tune_batch(dads, npg=16, candidates=(2, 4), repeats=1)
+    assert best in (2, 4) and set(times) == {2, 4}
+    assert api.batch_workers(dads, 16, "mixed") == best
+    x_tuned = solve_batch(dads, npg=16, nworkers=0)
+    x_two = solve_batch(make_batch(sizes), npg=16, nworkers=2)
+    # every domain runs the same kernels whichever worker takes it
+    for a, b in zip(x_tuned, x_two):
+        assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(b)
