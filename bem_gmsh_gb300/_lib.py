@@ -96,6 +96,9 @@ def load(build_if_missing: bool = False):
         "bem_adjoint_laplace2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, VP, VP, VP, ctypes.c_int, D, D,
                                    ctypes.c_int, ctypes.c_int, PD, VP, ctypes.POINTER(BemSolveStats)],
                                   ctypes.c_int),
+        "bem_adjoint_laplace2d_batch": ([ctx_p, ctypes.c_int, ctypes.POINTER(BemGeom2D), D, VP, VP, VP,
+                                         ctypes.POINTER(I64), ctypes.c_int, D, D, ctypes.c_int, VP, VP,
+                                         ctypes.c_int, ctypes.POINTER(BemSolveStats)], ctypes.c_int),
         "bem_solve2d_batch": ([ctx_p, ctypes.c_int, ctypes.POINTER(BemGeom2D), ctypes.c_int, D, D, VP, VP,
                                ctypes.POINTER(I64), ctypes.c_int, D, ctypes.c_int, D, ctypes.c_int,
                                ctypes.c_int, VP, ctypes.POINTER(I64), ctypes.c_int,

@@ -428,6 +428,59 @@ def adjoint_laplace(dad: BEMdata, q_target, npg: int = 16, near_factor: float = 
     return out
 
 
+def adjoint_laplace_batch(cases, npg: int = 16, near_factor: float = 1.5, tol: float = 1e-14,
+                          max_iter: int = 200, nworkers: int = 16, ctx: _lib.Context | None = None,
+                          return_stats: bool = False):
+    """`adjoint_laplace` for many independent domains in one call
+    (bem_adjoint_laplace2d_batch): `cases` is a sequence of (dad, q_target)
+    pairs sharing the conductivity of the first; worker threads with their
+    own streams overlap the domains.  Returns the list of (J, grad) (and the
+    per-domain stats)."""
+    cases = list(cases)
+    if not cases:
+        return ([], []) if return_stats else []
+    dads = [d for d, _ in cases]
+    k = dads[0].properties
+    for d in dads:
+        if not isinstance(d.properties, Laplace) or d.properties != k:
+            raise ValueError("adjoint_laplace_batch needs Laplace problems with the same conductivity")
+        if d.ngeo != 0 or d.nt != d.n:
+            raise ValueError("adjoint_laplace_batch needs node-interpolant elements (from_nodes) and no "
+                             "internal points")
+    qts = [np.asarray(q, dtype=np.float64).reshape(-1) for _, q in cases]
+    for d, q in zip(dads, qts):
+        if q.shape != (d.n,):
+            raise ValueError("q_target must have one value per boundary node")
+    ctx = ctx or _lib.default_context()
+    geoms = (_lib.BemGeom2D * len(dads))()
+    keep = []
+    for i, d in enumerate(dads):
+        g, kp = geom_struct(d, device=False)
+        geoms[i] = g
+        keep.append(kp)
+    lens = np.array([d.n for d in dads], np.int64)
+    off = np.zeros(len(dads), np.int64)
+    np.cumsum(lens[:-1], out=off[1:])
+    BC = np.ascontiguousarray(np.concatenate([np.asarray(d.BC, np.int32) for d in dads]))
+    BV = np.ascontiguousarray(np.concatenate([np.asarray(d.BV, np.float64) for d in dads]))
+    QT = np.ascontiguousarray(np.concatenate(qts))
+    J = np.zeros(len(dads))
+    grad = np.zeros(2 * int(lens.sum()))
+    stats = (_lib.BemSolveStats * len(dads))()
+    rc = ctx.L.bem_adjoint_laplace2d_batch(ctx.h, len(dads), geoms, float(k.k), _ptr(BC), _ptr(BV), _ptr(QT),
+                                           off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), int(npg),
+                                           float(near_factor), float(tol), int(max_iter), _ptr(J), _ptr(grad),
+                                           int(nworkers), stats)
+    if rc not in (_lib.BEM_OK, 4):
+        ctx.check(rc, "adjoint_laplace_batch")
+    out = [(float(J[i]), grad[2 * o:2 * (o + n)].reshape(n, 2).copy()) for i, (o, n) in enumerate(zip(off, lens))]
+    if return_stats:
+        st = [dict(status=s.status, iterations=s.iterations, t_assemble_ms=s.t_assemble_ms,
+                   t_factor_ms=s.t_factor_ms, t_refine_ms=s.t_refine_ms) for s in stats]
+        return out, st
+    return out
+
+
 RBF_KINDS = {"PHS1": 1, "PHS2": 2, "PHS3": 3, "PHS4": 4, "PHS5": 5, "PHS6": 6, "PHS7": 7, "fundamental": 10}
 
 

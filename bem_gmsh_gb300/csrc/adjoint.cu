@@ -344,30 +344,33 @@ extern "C" int bem_adjoint_laplace2d(bem_ctx* c, const bem_geom2d* g, double k, 
   // forward: fused assembly and mixed-precision solve
   double* A = (double*)c->get(bem_ctx::SLOT_OUT0, sizeof(double) * (size_t)ld * N);
   double* At = (double*)c->get(bem_ctx::SLOT_ADJ0, sizeof(double) * (size_t)ld * N);
-  // b, u, T, q, dJdu, lambda, target, J | gX, gn (2n each), gJ | BC, BV
-  double* v = (double*)c->get(bem_ctx::SLOT_ADJ1, sizeof(double) * (size_t)(14 * N + 64));
+  // b, u, T, q, dJdu, lambda (n each) | gX, gn (2n each), gJ | J | target, BV, BC (staged inputs)
+  double* v = (double*)c->get(bem_ctx::SLOT_ADJ1, sizeof(double) * (size_t)(15 * N + 64));
   if (!A || !At || !v) return BEM_ERR_NOMEM;
   double *b = v, *u = v + N, *T = v + 2 * N, *q = v + 3 * N, *dJdu = v + 4 * N, *lam = v + 5 * N;
-  double *qt = v + 6 * N, *gX = v + 7 * N, *gn = v + 9 * N, *gJ = v + 11 * N, *Jd = v + 12 * N;
-  if (mem == BEM_MEM_HOST)
-    cudaMemcpyAsync(qt, q_target, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
-  else
-    cudaMemcpyAsync(qt, q_target, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream);
-  const int prec = (c->opt_far_df >= 1) ? 3 : 1;
-  rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, prec, A, ld, nullptr, b);
-  if (rc) return rc;
-  // device copies of BC, BV for the split of the forward solution
+  double *gX = v + 7 * N, *gn = v + 9 * N, *gJ = v + 11 * N, *Jd = v + 12 * N;
+  double* stg = v + 12 * (size_t)N + 8;
+  double* qt = stg;
   const int32_t* dBC = BC;
   const double* dBV = BV;
   if (mem == BEM_MEM_HOST) {
-    int32_t* hbc = (int32_t*)c->get(bem_ctx::SLOT_BC, sizeof(int32_t) * (size_t)n);
-    double* hbv = (double*)c->get(bem_ctx::SLOT_BV, sizeof(double) * (size_t)n);
-    if (!hbc || !hbv) return BEM_ERR_NOMEM;
-    cudaMemcpyAsync(hbc, BC, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(hbv, BV, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
-    dBC = hbc;
-    dBV = hbv;
+    // target, BV, BC up in one copy through the pinned buffer
+    const size_t words = 2 * (size_t)N + ((size_t)N + 1) / 2;
+    double* h = (double*)c->pinned(words * sizeof(double));
+    if (!h) return BEM_ERR_NOMEM;
+    std::memcpy(h, q_target, sizeof(double) * (size_t)N);
+    std::memcpy(h + N, BV, sizeof(double) * (size_t)N);
+    std::memcpy(h + 2 * (size_t)N, BC, sizeof(int32_t) * (size_t)N);
+    cudaMemcpyAsync(stg, h, words * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    c->pin_issued();
+    dBV = stg + N;
+    dBC = (const int32_t*)(stg + 2 * (size_t)N);
+  } else {
+    cudaMemcpyAsync(qt, q_target, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream);
   }
+  const int prec = (c->opt_far_df >= 1) ? 3 : 1;
+  rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, prec, A, ld, nullptr, b);
+  if (rc) return rc;
   bem_solve_stats st{};
   rc = bem_solve_mixed_dev(c, N, A, ld, b, tol, max_iter, 1, u, &st);
   if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;
@@ -410,17 +413,24 @@ extern "C" int bem_adjoint_laplace2d(bem_ctx* c, const bem_geom2d* g, double k, 
   count_launches(4);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return c->cuda_fail(e, "adjoint kernels");
-  int hc[2] = {0, 0};
-  cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, c->stream);
+  // gradient, J and the pair counters back through the pinned buffer
+  double* hout = (double*)c->pinned(sizeof(double) * (2 * (size_t)N + 2));
+  if (!hout) return BEM_ERR_NOMEM;
+  const int* hc = (const int*)(hout + 2 * (size_t)N + 1);
+  cudaMemcpyAsync(hout + 2 * (size_t)N + 1, cnt, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (mem == BEM_MEM_HOST) {
-    cudaMemcpyAsync(grad, gX, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost, c->stream);
-    cudaMemcpyAsync(J, Jd, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(hout, gX, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(hout + 2 * (size_t)N, Jd, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
   } else {
     cudaMemcpyAsync(grad, gX, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToDevice, c->stream);
     cudaMemcpyAsync(J, Jd, sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   }
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return c->cuda_fail(e, "adjoint");
+  if (mem == BEM_MEM_HOST) {
+    std::memcpy(grad, hout, sizeof(double) * 2 * (size_t)N);
+    *J = hout[2 * (size_t)N];
+  }
   if (hc[1] != 0) {
     c->last_error = "adjoint: near-pair list overflow";
     return BEM_ERR_INTERNAL;

@@ -298,6 +298,19 @@ int bem_solve2d_batch(bem_ctx* ctx, int ndom, const bem_geom2d* geoms, int kind,
                       int nworkers, bem_solve_stats* stats);
 
 /*
+ * bem_adjoint_laplace2d for ndom independent domains on nworkers worker
+ * streams (0 = 8, at most 32), largest domains first; host buffers only.
+ * Domain d's BC, BV and q_target entries start at offset off[d] (n_d of
+ * each), its gradient at grad + 2 off[d] (2 n_d values) and its misfit is
+ * J[d].  stats (optional) receives one record per domain.  Returns as
+ * bem_solve2d_batch.  The call is synchronous.
+ */
+int bem_adjoint_laplace2d_batch(bem_ctx* ctx, int ndom, const bem_geom2d* geoms, double k, const int32_t* BC,
+                                const double* BV, const double* q_target, const int64_t* off, int npg,
+                                double near_factor, double tol, int max_iter, double* J, double* grad,
+                                int nworkers, bem_solve_stats* stats);
+
+/*
  * Laplace potential at m interior points from solved boundary data --
  * replaces `interior_laplace(dad, pf; T, q)` (src/Laplace/Lubrication.jl:399-416;
  * the same sum as `_interior_T`, test/laplace.jl:36-53): every element is

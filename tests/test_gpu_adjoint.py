@@ -70,3 +70,29 @@ def test_adjoint_gradient_c5_domain_sampled(orc):
     g_fd = fd_grad(orc, dad, qt, coords)
     scale = np.max(np.abs(g))
     assert np.max(np.abs(g[idx] - g_fd)) < 1e-5 * scale, (g[idx], g_fd)
+
+
+def test_adjoint_batch_matches_single_calls():
+    from bem_gmsh_gb300.api import adjoint_laplace_batch
+    cases = [star_adjoint_case(n_el, p=2, seed=s) for s, n_el in enumerate((40, 75, 21, 60, 33))]
+    qts = []
+    for _, tg in cases:
+        solve(tg, npg=16, mode="mixed")
+        qts.append(np.where(tg.BC == 0, tg.cache["x"], 0.0))
+    pairs = [(d, q) for (d, _), q in zip(cases, qts)]
+    out, st = adjoint_laplace_batch(pairs, npg=16, nworkers=3, return_stats=True)
+    assert len(out) == len(pairs) and all(s["status"] == 0 for s in st)
+    for (d, q), (J, g) in zip(pairs, out):
+        J1, g1 = adjoint_laplace(d, q, npg=16)
+        assert g.shape == (d.n, 2)
+        # same kernels per domain; row sums use FP64 atomics, so agree to rounding
+        assert abs(J - J1) <= 1e-10 * max(abs(J1), 1e-300)
+        assert np.linalg.norm(g - g1) <= 1e-9 * np.linalg.norm(g1)
+
+
+def test_adjoint_batch_rejects_bad_cases():
+    from bem_gmsh_gb300.api import adjoint_laplace_batch
+    d, tg = star_adjoint_case(20, p=2, seed=1)
+    with pytest.raises(ValueError):
+        adjoint_laplace_batch([(d, np.zeros(d.n + 1))])
+    assert adjoint_laplace_batch([]) == []
