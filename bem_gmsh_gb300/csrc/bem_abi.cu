@@ -321,8 +321,13 @@ int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& g
   if (mem == BEM_MEM_HOST) {
     std::memcpy(ew, g->elem_weight, sizeof(double) * nn);
   } else {
-    if (cudaMemcpy(ew, g->elem_weight, sizeof(double) * nn, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return c->cuda_fail(cudaGetLastError(), "elem_weight");
+    // the element weights set up the host-side rule tables
+    double* h = (double*)c->pinned(sizeof(double) * BEM_MAXNN);
+    if (!h) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(h, g->elem_weight, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return c->cuda_fail(e, "elem_weight");
+    std::memcpy(ew, h, sizeof(double) * nn);
   }
   build_rules(g, npg, ew, R);
   gd.nt = g->nt;
@@ -414,8 +419,10 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
     q.pair_cap = cap;
     int rc = bem::launch_assembly(q, c->stream);
     if (rc != 0) return c->cuda_fail((cudaError_t)rc, "launch_assembly");
-    int hc[2] = {0, 0};
-    cudaMemcpyAsync(hc, q.counters, sizeof(hc), cudaMemcpyDeviceToHost, c->stream);
+    // pair count and far-kernel status through the pinned buffer
+    int* hc = (int*)c->pinned(64);
+    if (!hc) return BEM_ERR_NOMEM;
+    cudaMemcpyAsync(hc, q.counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return c->cuda_fail(e, "assembly");
     if (hc[1] != 0) {
