@@ -53,3 +53,33 @@ def test_geometry_builders():
     pl = plate_with_hole()
     assert pl.n == (1024 + 342) * 3 and pl.ndof == 2
     assert int((pl.BC == 0).sum()) == 3
+
+
+def declared_arity():
+    """{name: number of parameters} of every function declared in include/*.h."""
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        txt = re.sub(r"//[^\n]*", "", txt)
+        for m in re.finditer(r"\b(bem_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_python_bindings_match_declared_arity():
+    # every ctypes binding passes exactly the parameters the header declares
+    from bem_gmsh_gb300 import _lib, _build
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    L = _lib.load()
+    arity = declared_arity()
+    assert arity.get("bem_adjoint_laplace2d_batch") == 16
+    checked = 0
+    for name, n in sorted(arity.items()):
+        f = getattr(L, name)
+        if f.argtypes is None:
+            continue
+        assert len(f.argtypes) == n, (name, len(f.argtypes), n)
+        checked += 1
+    assert checked >= 20
