@@ -42,3 +42,18 @@ def test_tuner_rejects_empty_input(fake_batch):
     dads = c4_domains(c4_node_counts(3, hi=200, seed=2))
     with pytest.raises(ValueError):
         api.tune_batch(dads, candidates=(0, 64))
+
+
+def test_adjoint_batch_argument_checks_run_on_the_host():
+    # rejected before any library call (no GPU needed)
+    import numpy as np
+    from bem_gmsh_gb300 import star_adjoint_case
+    from bem_gmsh_gb300.geometry import quadrado
+    d, _ = star_adjoint_case(20, p=2, seed=1)
+    assert api.adjoint_laplace_batch([]) == []
+    assert api.adjoint_laplace_batch([], return_stats=True) == ([], [])
+    with pytest.raises(ValueError):
+        api.adjoint_laplace_batch([(d, np.zeros(d.n + 1))])
+    with pytest.raises(ValueError):          # internal points are not supported
+        q = quadrado(ndiv=5)
+        api.adjoint_laplace_batch([(q, np.zeros(q.n))])

@@ -88,11 +88,3 @@ def test_adjoint_batch_matches_single_calls():
         # same kernels per domain; row sums use FP64 atomics, so agree to rounding
         assert abs(J - J1) <= 1e-10 * max(abs(J1), 1e-300)
         assert np.linalg.norm(g - g1) <= 1e-9 * np.linalg.norm(g1)
-
-
-def test_adjoint_batch_rejects_bad_cases():
-    from bem_gmsh_gb300.api import adjoint_laplace_batch
-    d, tg = star_adjoint_case(20, p=2, seed=1)
-    with pytest.raises(ValueError):
-        adjoint_laplace_batch([(d, np.zeros(d.n + 1))])
-    assert adjoint_laplace_batch([]) == []
