@@ -18,6 +18,7 @@ BEM_OPT_TCGEN05 = 1
 BEM_OPT_KERNEL_TIMING = 2
 BEM_OPT_FAR_DF = 3
 BEM_OPT_GRAPHS = 4
+BEM_NOALLOC_MAX_NT, BEM_NOALLOC_MAX_NE = 16384, 8192
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
                   "lu_panels", "lu_thin"]
 

@@ -83,10 +83,14 @@ extern "C" int bem_assemble_laplace2d_noalloc(const bem_geom2d* geom, double k, 
   if (rc) return rc;
 
   bem::AsmRequest q{};
+  // The element weights are read on the caller's stream, so that the read is
+  // ordered after whatever the caller's earlier work on that stream wrote
+  // (the weights feed the host-built quadrature tables).
   double ew[BEM_MAXNN];
-  if (cudaMemcpy(ew, geom->elem_weight, sizeof(double) * (geom->p + 1), cudaMemcpyDeviceToHost) !=
-      cudaSuccess)
+  if (cudaMemcpyAsync(ew, geom->elem_weight, sizeof(double) * (geom->p + 1), cudaMemcpyDeviceToHost,
+                      st) != cudaSuccess)
     return BEM_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return BEM_ERR_CUDA;
   bem_build_rules(geom, npg, ew, q.R);
   q.g.nt = geom->nt;
   q.g.n = geom->n;

@@ -205,7 +205,12 @@ int64_t bem_launch_count(void);
  * BEM_NOALLOC_BYTES inside the library, present on every GPU that loads the
  * library until the process exits.  Limits: nt <= BEM_NOALLOC_MAX_NT,
  * ne <= BEM_NOALLOC_MAX_NE, at most 24*BEM_NOALLOC_MAX_NT near pairs;
- * larger problems return BEM_ERR_UNSUPPORTED.  geom, H and G are device
+ * larger problems return BEM_ERR_UNSUPPORTED.  The size limits are checked
+ * before any device work; the near-pair limit is only known after the
+ * assembly ran, so when it is exceeded the call returns BEM_ERR_UNSUPPORTED
+ * with H and G written but undefined (the pairs beyond the limit keep far-field
+ * values).  The element weights are read on cuda_stream, after the caller's
+ * earlier work on it.  geom, H and G are device
  * pointers; work runs on cuda_stream (NULL = legacy default stream) and the
  * call returns when it is done.  The first call on each device looks up the
  * array's address (loading the module) and should precede any stream

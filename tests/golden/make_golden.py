@@ -1,7 +1,8 @@
 """Regenerate tests/golden/core_known_answers.json from the reference's own
 test files (read as text; the reference is Julia and cannot run here).
 
-Usage:  python tests/golden/make_golden.py [/path/to/reference]
+Usage:  python tests/golden/make_golden.py /path/to/reference
+        (or with the path in the environment variable BEM_REFERENCE_DIR)
 
 Each entry records the reference file and line it was read from.  Only
 numeric literals and thresholds are extracted; the closed-form identities the
@@ -12,7 +13,10 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BEM_REFERENCE_DIR")
+if not REF:
+    raise SystemExit("usage: make_golden.py /path/to/reference (the reference project root), "
+                     "or set BEM_REFERENCE_DIR")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "core_known_answers.json")
 
 

@@ -83,3 +83,11 @@ def test_python_bindings_match_declared_arity():
         assert len(f.argtypes) == n, (name, len(f.argtypes), n)
         checked += 1
     assert checked >= 20
+
+
+def test_python_constants_match_header_defines():
+    from bem_gmsh_gb300 import _lib
+    txt = open(os.path.join(ROOT, "include", "bem_gb300.h")).read()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(BEM_[A-Z0-9_]+)\s+(\d+)\b", txt)}
+    for name in ("BEM_NOALLOC_MAX_NT", "BEM_NOALLOC_MAX_NE"):
+        assert getattr(_lib, name) == defines[name], name
