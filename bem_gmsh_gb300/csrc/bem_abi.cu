@@ -9,6 +9,7 @@
 
 #include "../../include/bem_gb300.h"
 #include "bem_abi_internal.h"
+#include "bem_crmath.cuh"
 #include "bem_kernels.h"
 
 namespace bem {
@@ -27,38 +28,11 @@ using bem::Rules;
 // ---------------------------------------------------------------------------
 namespace {
 
-// Gauss-Legendre nodes (ascending) and weights: Newton on the three-term
-// recurrence in extended precision.
-void gauss_legendre(int n, double* x, double* w) {
-  const int m = (n + 1) / 2;
-  for (int i = 0; i < m; ++i) {
-    long double z = std::cos(3.14159265358979323846L * (i + 0.75L) / (n + 0.5L));
-    long double pp = 0;
-    for (int it = 0; it < 100; ++it) {
-      long double p1 = 1, p2 = 0;
-      for (int j = 1; j <= n; ++j) {
-        long double p3 = p2;
-        p2 = p1;
-        p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
-      }
-      pp = n * (z * p1 - p2) / (z * z - 1);
-      long double z1 = z;
-      z = z1 - p1 / pp;
-      if ((double)z == (double)z1 && it > 2) break;
-    }
-    long double p1 = 1, p2 = 0;
-    for (int j = 1; j <= n; ++j) {
-      long double p3 = p2;
-      p2 = p1;
-      p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
-    }
-    pp = n * (z * p1 - p2) / (z * z - 1);
-    x[n - 1 - i] = (double)z;
-    x[i] = -(double)z;
-    w[i] = w[n - 1 - i] = (double)(2.0L / ((1 - z * z) * pp * pp));
-  }
-  if (n % 2 == 1) x[n / 2] = 0.0;
-}
+// Gauss-Legendre nodes (ascending) and weights, correctly rounded (Newton in
+// double-double arithmetic, bem_crmath.cuh): the tanp3c map amplifies a
+// one-ulp change of a node, so every implementation of the assembly must use
+// the same bits, and correct rounding is the one platform-independent choice.
+void gauss_legendre(int n, double* x, double* w) { bem::crm::gauss_legendre_cr(n, x, w); }
 
 // differentiation matrix of a barycentric basis (Interpolation.jl:193-213)
 void diff_matrix(const double* x, const double* bw, int n, double* D) {

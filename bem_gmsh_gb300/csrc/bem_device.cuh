@@ -14,6 +14,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "bem_nearmap.cuh"
+
 #define BEM_MAXNN 6     // field nodes per element (degree <= 5)
 #define BEM_MAXGEO 6    // CAD nodes per element
 #define BEM_MAXNPG 32   // near-field Gauss rule
@@ -279,83 +281,17 @@ __device__ inline void closest_point_1d(const Rules& R, const V2* nodes, int n, 
 }
 
 // --------------------------------------------------------------------------
-// complex arithmetic for the pole
+// complex pole and tanp3c map: exactly specified IEEE arithmetic and
+// correctly rounded atan/tan/cbrt (bem_nearmap.cuh), so that the map's
+// nodes and weights are the same bits as a CPU restatement's
 // --------------------------------------------------------------------------
-struct C2 {
-  double re, im;
-};
-__device__ __forceinline__ C2 cadd(C2 a, C2 b) { return {a.re + b.re, a.im + b.im}; }
-__device__ __forceinline__ C2 csub(C2 a, C2 b) { return {a.re - b.re, a.im - b.im}; }
-__device__ __forceinline__ C2 cmul(C2 a, C2 b) {
-  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
-}
-__device__ __forceinline__ C2 cscale(C2 a, double s) { return {a.re * s, a.im * s}; }
-__device__ __forceinline__ double cabs(C2 a) { return hypot(a.re, a.im); }
-// Smith's algorithm
-__device__ __forceinline__ C2 cdiv(C2 a, C2 b) {
-  if (fabs(b.re) >= fabs(b.im)) {
-    double r = b.im / b.re, d = b.re + b.im * r;
-    return {(a.re + a.im * r) / d, (a.im - a.re * r) / d};
-  }
-  double r = b.re / b.im, d = b.re * r + b.im;
-  return {(a.re * r + a.im) / d, (a.im * r - a.re) / d};
-}
-// principal square root
-__device__ __forceinline__ C2 csqrt(C2 z) {
-  if (z.re == 0.0 && z.im == 0.0) return {0.0, z.im};
-  double r = hypot(z.re, z.im);
-  if (z.re >= 0) {
-    double t = sqrt(0.5 * (r + z.re));
-    return {t, z.im / (2 * t)};
-  }
-  double t = sqrt(0.5 * (r - z.re));
-  return {fabs(z.im) / (2 * t), copysign(t, z.im)};
-}
-
 // _complex_pole_1d (Integration.jl:1117-1160)
 __device__ inline void complex_pole_1d(const Rules& R, const V2* nodes, int nN, V2 pf, double& z0,
                                 double& e0) {
-  C2 y{pf.x, pf.y};
-  if (nN == 2) {
-    double d = R.leg_x[1] - R.leg_x[0] + 1e-30;
-    C2 B{(nodes[1].x - nodes[0].x) / d, (nodes[1].y - nodes[0].y) / d};
-    C2 C = csub(C2{nodes[0].x, nodes[0].y}, cscale(B, R.leg_x[0]));
-    if (cabs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
-    C2 r = cdiv(csub(y, C), B);
-    z0 = r.re;
-    e0 = fabs(r.im);
-    return;
-  }
-  if (nN == 3) {
-    const double* xs = R.leg_x;
-    double a11 = xs[0] * xs[0], a12 = xs[0], a13 = 1;
-    double a21 = xs[1] * xs[1], a22 = xs[1], a23 = 1;
-    double a31 = xs[2] * xs[2], a32 = xs[2], a33 = 1;
-    double det = a11 * (a22 * a33 - a23 * a32) - a12 * (a21 * a33 - a23 * a31) +
-                 a13 * (a21 * a32 - a22 * a31);
-    C2 Z0{nodes[0].x, nodes[0].y}, Z1{nodes[1].x, nodes[1].y}, Z2{nodes[2].x, nodes[2].y};
-    C2 A = cscale(cadd(cadd(cscale(Z0, a22 * a33 - a23 * a32), cscale(Z1, a13 * a32 - a12 * a33)),
-                       cscale(Z2, a12 * a23 - a13 * a22)), 1.0 / det);
-    C2 B = cscale(cadd(cadd(cscale(Z0, a23 * a31 - a21 * a33), cscale(Z1, a11 * a33 - a13 * a31)),
-                       cscale(Z2, a13 * a21 - a11 * a23)), 1.0 / det);
-    C2 C = cscale(cadd(cadd(cscale(Z0, a21 * a32 - a22 * a31), cscale(Z1, a12 * a31 - a11 * a32)),
-                       cscale(Z2, a11 * a22 - a12 * a21)), 1.0 / det);
-    if (cabs(A) < 1e-14) {
-      if (cabs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
-      C2 r = cdiv(csub(y, C), B);
-      z0 = r.re;
-      e0 = fabs(r.im);
-      return;
-    }
-    C2 disc = csqrt(csub(cmul(B, B), cscale(cmul(A, csub(C, y)), 4.0)));
-    C2 twoA = cscale(A, 2.0);
-    C2 mB{-B.re, -B.im};
-    C2 r1 = cdiv(cadd(mB, disc), twoA);
-    C2 r2 = cdiv(csub(mB, disc), twoA);
-    C2 r = fabs(r1.im) <= fabs(r2.im) ? r1 : r2;
-    z0 = r.re;
-    e0 = fabs(r.im);
-    return;
+  if (nN <= 3) {
+    double nx[3], ny[3];
+    for (int k = 0; k < nN; ++k) { nx[k] = nodes[k].x; ny[k] = nodes[k].y; }
+    if (nm::complex_pole(R, nx, ny, nN, pf.x, pf.y, z0, e0)) return;
   }
   double a, dist;
   closest_point_1d(R, nodes, nN, pf, a, dist);
@@ -366,168 +302,9 @@ __device__ inline void complex_pole_1d(const Rules& R, const V2* nodes, int nN, 
   e0 = dist / fmax(vnorm(dx.x, dx.y), 1e-14);
 }
 
-// --------------------------------------------------------------------------
-// tanp3c map (Integration.jl:1163-1365).  Writes up to 2*npg nodes; returns
-// the count.
-// --------------------------------------------------------------------------
-__device__ __forceinline__ bool eq41_collinear(double z0, double e0, bool has_den, double den) {
-  if (fabs(z0) <= 1) return false;
-  if (fabs(e0) < 1e-8) return true;
-  if (has_den && fabs(den) < 1e-10) return true;
-  return false;
-}
-
-__device__ inline int eq41_real_pole(const Rules& R, double z0, double* x, double* wx) {
-  int m = R.npg;
-  if (fabs(z0) <= 1) {
-    for (int i = 0; i < m; ++i) { x[i] = R.qsi[i]; wx[i] = R.w[i]; }
-    return m;
-  }
-  double A = z0 * z0 - 1, B = -z0;
-  for (int i = 0; i < m; ++i) {
-    double d = R.qsi[i] - B;
-    x[i] = z0 - A / d;
-    wx[i] = R.w[i] * (A / (d * d));
-  }
-  return m;
-}
-
-__device__ inline int tangenttrans(const Rules& R, double z0, double e0, double* x, double* wx) {
-  if (eq41_collinear(z0, e0, false, 0.0)) return eq41_real_pole(R, z0, x, wx);
-  e0 = fmax(e0, 1e-14);
-  double tp = atan((1 - z0) / e0), tm = atan((-1 - z0) / e0);
-  double den = tp - tm;
-  if (eq41_collinear(z0, e0, true, den)) return eq41_real_pole(R, z0, x, wx);
-  double A = 2.0 * e0 / den, B = -(tp + tm) / den;
-  double halfpi = kPi / 2 - 1e-8;
-  for (int i = 0; i < R.npg; ++i) {
-    double phi = fmin(fmax(e0 * (R.qsi[i] - B) / A, -halfpi), halfpi);
-    double tn = tan(phi);
-    x[i] = z0 + e0 * tn;
-    wx[i] = R.w[i] * ((e0 * e0 / A) * (1 + tn * tn));
-  }
-  return R.npg;
-}
-
-__device__ __forceinline__ double jsign(double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); }
-
-// _p3c_inv_pole (Integration.jl:1220-1270)
-__device__ inline void p3c_inv_pole(double z0, double e0, double& zt, double& et) {
-  if (fabs(e0) < 1e-14) {
-    double x = z0;
-    for (int it = 0; it < 25; ++it) {
-      double g = x * x * x - 3 * z0 * (x * x) + 3 * x - z0;
-      double gp = 3 * (x * x) - 6 * z0 * x + 3;
-      if (fabs(gp) < 1e-30) break;
-      x -= g / gp;
-      if (fabs(g) < 1e-14) break;
-    }
-    zt = x;
-    et = 0.0;
-    return;
-  }
-  double e = cbrt(fabs(e0)) * jsign(e0);
-  for (int it = 0; it < 20; ++it) {
-    double g = 2 * (e * e * e) - 3 * e0 * (e * e) - e0;
-    double gp = 6 * (e * e) - 6 * e0 * e;
-    if (fabs(gp) < 1e-30) break;
-    e -= g / gp;
-  }
-  e += cbrt(e0) * sqrt(z0 * z0 + e0 * e0);
-  double z = z0;
-  for (int it = 0; it < 30; ++it) {
-    double den = 1 + 3 * (z * z) + 3 * (e * e);
-    double nz = (3 + z * z + 3 * (e * e)) * z;
-    double ne = 2 * (e * e * e);
-    double f1 = nz / den - z0, f2 = ne / den - e0;
-    if (fabs(f1) + fabs(f2) < 1e-14) break;
-    double denz = 6 * z, dene = 6 * e;
-    double nz_z = 3 + 3 * (z * z) + 3 * (e * e);
-    double nz_e = 6 * e * z;
-    double ne_e = 6 * (e * e);
-    double den2 = den * den;
-    double j11 = (nz_z * den - nz * denz) / den2;
-    double j12 = (nz_e * den - nz * dene) / den2;
-    double j21 = (0.0 * den - ne * denz) / den2;
-    double j22 = (ne_e * den - ne * dene) / den2;
-    double det = j11 * j22 - j12 * j21;
-    if (fabs(det) < 1e-30) break;
-    z -= (j22 * f1 - j12 * f2) / det;
-    e -= (-j21 * f1 + j11 * f2) / det;
-  }
-  zt = z;
-  et = e;
-}
-
-// p3c map of the npg rule, then the affine chart u = mid + h s and the
-// tangent map; appends to x/wx at offset `off`.  (_p3ctrans,
-// _tanp3c_compose, _tanp3c_half)
-__device__ inline int p3c_tangent_piece(const Rules& R, double spole, double mid, double h, double z0,
-                                 double e0, double At, double Bt, double* x, double* wx, int off) {
-  double zt, et;
-  p3c_inv_pole(spole, 1e-14, zt, et);
-  double den = 1 + 3 * (zt * zt) + 3 * (et * et);
-  double A = 3.0 / den;
-  double B = (3 + zt * zt) * zt / den;
-  double halfpi = kPi / 2 - 1e-8;
-  for (int i = 0; i < R.npg; ++i) {
-    double s = R.qsi[i];
-    double ds = s - zt;
-    double sm = A * ((ds * ds * ds) / 3 + (et * et) * s) + B;
-    double ws = R.w[i] * (A * ((ds * ds) + et * et));
-    double ut = mid + h * sm;
-    ws = ws * h;
-    double th = fmin(fmax((ut - Bt) / At, -halfpi), halfpi);
-    double tn = tan(th);
-    x[off + i] = z0 + e0 * tn;
-    wx[off + i] = ws * ((e0 / At) * (1 + tn * tn));
-  }
-  return R.npg;
-}
-
-__device__ inline int p3ctrans(const Rules& R, double z0, double e0, double* x, double* wx) {
-  double zt, et;
-  p3c_inv_pole(z0, e0, zt, et);
-  double den = 1 + 3 * (zt * zt) + 3 * (et * et);
-  double A = 3.0 / den, B = (3 + zt * zt) * zt / den;
-  for (int i = 0; i < R.npg; ++i) {
-    double s = R.qsi[i], ds = s - zt;
-    x[i] = A * ((ds * ds * ds) / 3 + (et * et) * s) + B;
-    wx[i] = R.w[i] * (A * ((ds * ds) + et * et));
-  }
-  return R.npg;
-}
-
-// _tanp3ctrans.  A split half narrower than 1e-14 contributes no nodes (the
-// reference gives it the full-interval tangent rule, counting the element
-// twice; see Integration.jl:1349).
+// _tanp3ctrans (Integration.jl:1290-1365): up to 2*npg nodes, returns the count
 __device__ inline int tanp3ctrans(const Rules& R, double z0, double e0, double* x, double* wx) {
-  if (eq41_collinear(z0, e0, false, 0.0)) return eq41_real_pole(R, z0, x, wx);
-  e0 = fmax(e0, 1e-14);
-  double ap = atan((1 - z0) / e0), am = atan((1 + z0) / e0);
-  double den = ap + am;
-  if (eq41_collinear(z0, e0, true, den)) return eq41_real_pole(R, z0, x, wx);
-  if (fabs(den) < 1e-30) return p3ctrans(R, z0, e0, x, wx);
-  double At = 2.0 / den;
-  double Bt = -At * (ap - am) / 2.0;
-  double uL = Bt - At * kPi / 2, uR = Bt + At * kPi / 2;
-  if (fabs(z0) < 1 && -1 < Bt && Bt < 1) {
-    int m = 0;
-    // left half [-1, Bt]
-    {
-      double lo = -1.0, hi = Bt;
-      double mid = (hi + lo) / 2, h = (hi - lo) / 2;
-      if (h > 1e-14) m += p3c_tangent_piece(R, (uL - mid) / h, mid, h, z0, e0, At, Bt, x, wx, m);
-    }
-    {
-      double lo = Bt, hi = 1.0;
-      double mid = (hi + lo) / 2, h = (hi - lo) / 2;
-      if (h > 1e-14) m += p3c_tangent_piece(R, (uR - mid) / h, mid, h, z0, e0, At, Bt, x, wx, m);
-    }
-    return m;
-  }
-  double upole = (z0 >= 1) ? uL : uR;
-  return p3c_tangent_piece(R, upole, 0.0, 1.0, z0, e0, At, Bt, x, wx, 0);
+  return nm::tanp3ctrans(R, z0, e0, x, wx);
 }
 
 // --------------------------------------------------------------------------

@@ -10,6 +10,18 @@
 // the oracle agrees with the reference to a few ulps.  Build it with
 // -ffp-contract=off: Julia does not fuse a*b+c into an FMA.
 //
+// Elementary functions on the near-singular map (atan, tan, cbrt) and the
+// Gauss-Legendre rules are correctly rounded here: evaluated in IEEE quad
+// precision (113-bit; __float128 with libquadmath on x86-64, long double on
+// aarch64) and rounded once to double.  The reference's tanp3c map turns a
+// one-ulp change of one of these values into up to ~5e-5 relative change of
+// an element integral, so its result depends on the libm that evaluates it;
+// a correctly rounded value is the one result every correctly rounding
+// library returns (the reference's Julia libm, < 1 ulp, agrees with it for
+// all but a small fraction of arguments).  Complex arithmetic on that path
+// follows the algorithms of Julia's Complex{Float64} (product ac - bd,
+// ad + bc; Baudin-Smith robust quotient; Kahan's square root).
+//
 // Layout conventions (same as the C-ABI of the CUDA library):
 //   * elements are discontinuous: element e owns boundary nodes
 //     e*(p+1) .. e*(p+1)+p, collocation points are boundary nodes first
@@ -18,6 +30,7 @@
 //     rows x cols with rows = dof*nt, cols = dof*n (dof = 1 Laplace, 2 Kelvin).
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -28,9 +41,32 @@
 #include <omp.h>
 #endif
 
+#if defined(__x86_64__) || defined(__i386__)
+#include <quadmath.h>
+typedef __float128 qreal;
+static inline qreal q_atan(qreal x) { return atanq(x); }
+static inline qreal q_tan(qreal x) { return tanq(x); }
+static inline qreal q_cbrt(qreal x) { return cbrtq(x); }
+static inline qreal q_cos(qreal x) { return cosq(x); }
+static inline qreal q_fabs(qreal x) { return fabsq(x); }
+#else
+static_assert(LDBL_MANT_DIG == 113, "the oracle needs IEEE quad precision long double on this platform");
+typedef long double qreal;
+static inline qreal q_atan(qreal x) { return atanl(x); }
+static inline qreal q_tan(qreal x) { return tanl(x); }
+static inline qreal q_cbrt(qreal x) { return cbrtl(x); }
+static inline qreal q_cos(qreal x) { return cosl(x); }
+static inline qreal q_fabs(qreal x) { return fabsl(x); }
+#endif
+
 namespace {
 
 constexpr double kPi = 3.141592653589793;
+
+// correctly rounded atan, tan, cbrt (quad precision rounded once)
+double cr_atan(double x) { return (double)q_atan((qreal)x); }
+double cr_tan(double x) { return (double)q_tan((qreal)x); }
+double cr_cbrt(double x) { return (double)q_cbrt((qreal)x); }
 constexpr double kEps = 2.220446049250313e-16;  // eps(Float64)
 using cplx = std::complex<double>;
 
@@ -38,38 +74,42 @@ using cplx = std::complex<double>;
 // Gauss-Legendre rule.  FastGaussQuadrature 1.3.0 `gausslegendre(n)` (a
 // third-party dependency, called at src/Core/Assembly_full.jl:720,
 // src/Core/Input.jl:88, src/Core/Integration.jl:1599).  Restated as Newton on
-// the Legendre three-term recurrence in extended precision, ascending nodes.
+// the Legendre three-term recurrence in quad precision, ascending nodes,
+// nodes and weights correctly rounded.
 // ---------------------------------------------------------------------------
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
   x.assign(n, 0.0);
   w.assign(n, 0.0);
   const int m = (n + 1) / 2;
+  const qreal pi = (qreal)3.14159265358979323846264338327950288L;
   for (int i = 0; i < m; ++i) {
-    long double z = std::cos(kPi * (i + 0.75L) / (n + 0.5L));
-    long double pp = 0;
-    for (int it = 0; it < 100; ++it) {
-      long double p1 = 1, p2 = 0;
+    qreal z = q_cos(pi * ((qreal)i + (qreal)0.75) / ((qreal)n + (qreal)0.5));
+    qreal pp = 0;
+    auto eval = [&](qreal zz, qreal& p1, qreal& dp) {
+      qreal a = 1, b = 0;
       for (int j = 1; j <= n; ++j) {
-        long double p3 = p2;
-        p2 = p1;
-        p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
+        qreal c = b;
+        b = a;
+        a = ((2 * (qreal)j - 1) * zz * b - ((qreal)j - 1) * c) / (qreal)j;
       }
-      pp = n * (z * p1 - p2) / (z * z - 1);
-      long double z1 = z;
-      z = z1 - p1 / pp;
-      if (std::fabs((double)(z - z1)) == 0.0 && it > 2) break;
-    }
-    {
-      long double p1 = 1, p2 = 0;
-      for (int j = 1; j <= n; ++j) {
-        long double p3 = p2;
-        p2 = p1;
-        p1 = ((2.0L * j - 1) * z * p2 - (j - 1.0L) * p3) / j;
+      p1 = a;
+      dp = (qreal)n * (zz * a - b) / (zz * zz - 1);
+    };
+    if (n % 2 == 1 && i == m - 1) {
+      z = 0;
+    } else {
+      for (int it = 0; it < 100; ++it) {
+        qreal p1;
+        eval(z, p1, pp);
+        qreal dz = p1 / pp;
+        z -= dz;
+        if (q_fabs(dz) <= (qreal)1e-33 * q_fabs(z)) break;
       }
-      pp = n * (z * p1 - p2) / (z * z - 1);
     }
+    qreal p1;
+    eval(z, p1, pp);
     double xi = (double)z;
-    double wi = (double)(2.0L / ((1 - z * z) * pp * pp));
+    double wi = (double)((qreal)2 / ((1 - z * z) * pp * pp));
     x[n - 1 - i] = xi;
     x[i] = -xi;
     w[i] = wi;
@@ -449,8 +489,8 @@ void eq41_real_pole(const Rule& u, const Rule& w, double z0, Rule& x, Rule& wx) 
 void tangenttrans(const Rule& u, const Rule& w, double z0, double e0, Rule& x, Rule& wx) {
   if (eq41_collinear(z0, e0)) { eq41_real_pole(u, w, z0, x, wx); return; }
   e0 = std::max(e0, 1e-14);
-  double tp = std::atan((1 - z0) / e0);
-  double tm = std::atan((-1 - z0) / e0);
+  double tp = cr_atan((1 - z0) / e0);
+  double tm = cr_atan((-1 - z0) / e0);
   double den = tp - tm;
   if (eq41_collinear(z0, e0, true, den)) { eq41_real_pole(u, w, z0, x, wx); return; }
   double A = 2.0 * e0 / den;
@@ -460,7 +500,7 @@ void tangenttrans(const Rule& u, const Rule& w, double z0, double e0, Rule& x, R
   wx.resize(u.size());
   for (size_t i = 0; i < u.size(); ++i) {
     double phi = std::min(std::max(e0 * (u[i] - B) / A, -halfpi), halfpi);
-    double tn = std::tan(phi);
+    double tn = cr_tan(phi);
     x[i] = z0 + e0 * tn;
     wx[i] = w[i] * ((e0 * e0 / A) * (1 + tn * tn));
   }
@@ -481,14 +521,14 @@ void p3c_inv_pole(double z0, double e0, double& zt, double& et) {
     et = 0.0;
     return;
   }
-  double e = std::cbrt(std::fabs(e0)) * jsign(e0);
+  double e = cr_cbrt(std::fabs(e0)) * jsign(e0);
   for (int it = 0; it < 20; ++it) {
     double g = 2 * (e * e * e) - 3 * e0 * (e * e) - e0;
     double gp = 6 * (e * e) - 6 * e0 * e;
     if (std::fabs(gp) < 1e-30) break;
     e -= g / gp;
   }
-  e += std::cbrt(e0) * std::sqrt(z0 * z0 + e0 * e0);
+  e += cr_cbrt(e0) * std::sqrt(z0 * z0 + e0 * e0);
   double z = z0;
   for (int it = 0; it < 30; ++it) {
     double den = 1 + 3 * (z * z) + 3 * (e * e);
@@ -540,7 +580,7 @@ void tanp3c_tail(const Rule& ut, const Rule& wt, double z0, double e0, double At
   wx.resize(m);
   for (size_t i = 0; i < m; ++i) {
     double th = std::min(std::max((ut[i] - Bt) / At, -halfpi), halfpi);
-    double tn = std::tan(th);
+    double tn = cr_tan(th);
     x[i] = z0 + e0 * tn;
     wx[i] = wt[i] * ((e0 / At) * (1 + tn * tn));
   }
@@ -584,8 +624,8 @@ void tanp3c_half(const Rule& u, const Rule& w, double z0, double e0, double At, 
 void tanp3ctrans(const Rule& u, const Rule& w, double z0, double e0, Rule& x, Rule& wx) {
   if (eq41_collinear(z0, e0)) { eq41_real_pole(u, w, z0, x, wx); return; }
   e0 = std::max(e0, 1e-14);
-  double ap = std::atan((1 - z0) / e0);
-  double am = std::atan((1 + z0) / e0);
+  double ap = cr_atan((1 - z0) / e0);
+  double am = cr_atan((1 + z0) / e0);
   double den = ap + am;
   if (eq41_collinear(z0, e0, true, den)) { eq41_real_pole(u, w, z0, x, wx); return; }
   if (std::fabs(den) < 1e-30) { p3ctrans(u, w, z0, e0, x, wx); return; }
@@ -608,51 +648,106 @@ void tanp3ctrans(const Rule& u, const Rule& w, double z0, double e0, Rule& x, Ru
   }
 }
 
+// Complex{Float64} arithmetic as Julia evaluates it: the product
+// (ac - bd, ad + bc), componentwise scaling by a real, the quotient by
+// Baudin and Smith's robust Smith method ("A robust complex division in
+// Scilab", 2012; its over/underflow rescaling is left out: element-size
+// operands never come near those thresholds), and the square root by
+// Kahan's method ("Branch cuts for complex elementary functions", 1987;
+// rescaling left out for the same reason).  abs is hypot.
+struct jc {
+  double re, im;
+};
+jc jadd(jc a, jc b) { return {a.re + b.re, a.im + b.im}; }
+jc jsub(jc a, jc b) { return {a.re - b.re, a.im - b.im}; }
+jc jmul(jc a, jc b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+jc jscale(double s, jc a) { return {s * a.re, s * a.im}; }
+jc jdivr(jc a, double s) { return {a.re / s, a.im / s}; }
+double jabs(jc a) { return std::hypot(a.re, a.im); }
+
+// one half of the robust quotient: (a + ib) / (c + id) with |d| <= |c|
+double jdiv_part(double a, double b, double c, double d, double r, double t) {
+  if (r != 0) {
+    double br = b * r;
+    return br != 0 ? (a + br) * t : a * t + (b * t) * r;
+  }
+  return (a + d * (b / c)) * t;
+}
+jc jdiv(jc x, jc y) {
+  double a = x.re, b = x.im, c = y.re, d = y.im;
+  if (std::fabs(d) <= std::fabs(c)) {
+    double r = d / c, t = 1.0 / (c + d * r);
+    return {jdiv_part(a, b, c, d, r, t), jdiv_part(b, -a, c, d, r, t)};
+  }
+  double r = c / d, t = 1.0 / (d + c * r);
+  return {jdiv_part(b, a, d, c, r, t), -jdiv_part(a, -b, d, c, r, t)};
+}
+jc jsqrt(jc z) {
+  double x = z.re, y = z.im;
+  if (x == 0 && y == 0) return {0.0, y};
+  double rho = x * x + y * y;
+  rho = std::fabs(x) + std::sqrt(rho);
+  rho += rho;
+  rho = std::sqrt(rho) * 0.5;
+  double xi = rho, eta = y;
+  if (rho != 0) {
+    eta = (eta / rho) / 2;
+    if (x < 0) {
+      xi = std::fabs(eta);
+      eta = std::copysign(rho, y);
+    }
+  }
+  return {xi, eta};
+}
+
 // _complex_pole_1d (Integration.jl:1117-1160)
 void complex_pole_1d(const Poly& P, const V2* nodes, int nN, V2 pf, double& z0, double& e0) {
-  cplx y(pf.x, pf.y);
+  jc y{pf.x, pf.y};
   if (nN == 2 || nN == 3) {
     std::vector<double> xs(P.nodes.begin(), P.nodes.end());
     if ((int)xs.size() != nN) {
       xs.resize(nN);
       for (int k = 0; k < nN; ++k) xs[k] = -1.0 + 2.0 * k / (nN - 1);
     }
-    cplx Z[3];
-    for (int k = 0; k < nN; ++k) Z[k] = cplx(nodes[k].x, nodes[k].y);
+    jc Z[3];
+    for (int k = 0; k < nN; ++k) Z[k] = jc{nodes[k].x, nodes[k].y};
     if (nN == 2) {
-      cplx B = (Z[1] - Z[0]) / (xs[1] - xs[0] + 1e-30);
-      cplx C = Z[0] - B * xs[0];
-      if (std::abs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
-      cplx r = (y - C) / B;
-      z0 = r.real();
-      e0 = std::fabs(r.imag());
+      jc B = jdivr(jsub(Z[1], Z[0]), xs[1] - xs[0] + 1e-30);
+      jc C = jsub(Z[0], jscale(xs[0], B));
+      if (jabs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
+      jc r = jdiv(jsub(y, C), B);
+      z0 = r.re;
+      e0 = std::fabs(r.im);
       return;
     }
-    // Vandermonde [xi^2 xi 1] \ Z by Cramer's rule (_fit_quad_complex)
+    // Vandermonde [xi^2 xi 1] \ Z by cofactors over the determinant
+    // (_fit_quad_complex: the closed form StaticArrays uses for 3x3 solves)
     double a11 = xs[0] * xs[0], a12 = xs[0], a13 = 1;
     double a21 = xs[1] * xs[1], a22 = xs[1], a23 = 1;
     double a31 = xs[2] * xs[2], a32 = xs[2], a33 = 1;
     double det = a11 * (a22 * a33 - a23 * a32) - a12 * (a21 * a33 - a23 * a31) +
                  a13 * (a21 * a32 - a22 * a31);
-    cplx A = ((a22 * a33 - a23 * a32) * Z[0] + (a13 * a32 - a12 * a33) * Z[1] +
-              (a12 * a23 - a13 * a22) * Z[2]) / det;
-    cplx B = ((a23 * a31 - a21 * a33) * Z[0] + (a11 * a33 - a13 * a31) * Z[1] +
-              (a13 * a21 - a11 * a23) * Z[2]) / det;
-    cplx C = ((a21 * a32 - a22 * a31) * Z[0] + (a12 * a31 - a11 * a32) * Z[1] +
-              (a11 * a22 - a12 * a21) * Z[2]) / det;
-    if (std::abs(A) < 1e-14) {
-      if (std::abs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
-      cplx r = (y - C) / B;
-      z0 = r.real();
-      e0 = std::fabs(r.imag());
+    auto comb = [&](double c0, double c1, double c2) {
+      return jdivr(jadd(jadd(jscale(c0, Z[0]), jscale(c1, Z[1])), jscale(c2, Z[2])), det);
+    };
+    jc A = comb(a22 * a33 - a23 * a32, a13 * a32 - a12 * a33, a12 * a23 - a13 * a22);
+    jc B = comb(a23 * a31 - a21 * a33, a11 * a33 - a13 * a31, a13 * a21 - a11 * a23);
+    jc C = comb(a21 * a32 - a22 * a31, a12 * a31 - a11 * a32, a11 * a22 - a12 * a21);
+    if (jabs(A) < 1e-14) {
+      if (jabs(B) < 1e-30) { z0 = 0.0; e0 = 1.0; return; }
+      jc r = jdiv(jsub(y, C), B);
+      z0 = r.re;
+      e0 = std::fabs(r.im);
       return;
     }
-    cplx disc = std::sqrt(B * B - 4.0 * A * (C - y));
-    cplx r1 = (-B + disc) / (2.0 * A);
-    cplx r2 = (-B - disc) / (2.0 * A);
-    cplx r = std::fabs(r1.imag()) <= std::fabs(r2.imag()) ? r1 : r2;
-    z0 = r.real();
-    e0 = std::fabs(r.imag());
+    jc disc = jsqrt(jsub(jmul(B, B), jmul(jscale(4.0, A), jsub(C, y))));
+    jc mB{-B.re, -B.im};
+    jc twoA = jscale(2.0, A);
+    jc r1 = jdiv(jadd(mB, disc), twoA);
+    jc r2 = jdiv(jsub(mB, disc), twoA);
+    jc r = std::fabs(r1.im) <= std::fabs(r2.im) ? r1 : r2;
+    z0 = r.re;
+    e0 = std::fabs(r.im);
     return;
   }
   double a, dist;
@@ -1230,6 +1325,37 @@ int orc_integrate_element(const OrcGeom* og, int kind, double prm0, double prm1,
   C.singular = singular;
   integrate_element(C, e, V2{pfx, pfy}, source, h, g);
   return 0;
+}
+
+// Correctly rounded atan (which = 0), tan (1), cbrt (2) of x[0..n-1].
+void orc_cr_fn(int which, const double* x, int n, double* out) {
+  for (int i = 0; i < n; ++i)
+    out[i] = which == 0 ? cr_atan(x[i]) : (which == 1 ? cr_tan(x[i]) : cr_cbrt(x[i]));
+}
+
+// The near-field rule (mapped nodes eta, weights w; up to 2 npg of them) that
+// integrate_element uses for element e and source point pf, with the pole
+// (z0, e0) it came from; returns the number of nodes.
+int orc_near_rule(const OrcGeom* og, int npg, int nearfield, int e, double pfx, double pfy, double* eta,
+                  double* w, double* z0e0) {
+  Geom gg = to_geom(og);
+  Ctx C;
+  setup_ctx(C, &gg, npg);
+  C.nearfield = nearfield;
+  const int nn = C.leg.np;
+  V2 nodes[16];
+  for (int k = 0; k < nn; ++k) nodes[k] = V2{gg.px[e * nn + k], gg.py[e * nn + k]};
+  double z0, e0;
+  complex_pole_1d(C.leg, nodes, nn, V2{pfx, pfy}, z0, e0);
+  z0e0[0] = z0;
+  z0e0[1] = e0;
+  Rule x, wx;
+  near_rule(C, nodes, V2{pfx, pfy}, gg.elen[e], x, wx);
+  for (size_t i = 0; i < x.size(); ++i) {
+    eta[i] = x[i];
+    w[i] = wx[i];
+  }
+  return (int)x.size();
 }
 
 // Near classification mask, nt x ne (row-major by collocation row).

@@ -79,6 +79,9 @@ def lib():
         _lib.orc_dibem_fd2d.argtypes = [i, P, P, i, d, d, i, d, P, P]
         _lib.orc_dibem_ifid2d.argtypes = [ctypes.POINTER(OrcGeom), d, i, d, d, P, P]
         _lib.orc_dibem_ifid2d.restype = i
+        _lib.orc_cr_fn.argtypes = [i, P, i, P]
+        _lib.orc_near_rule.argtypes = [ctypes.POINTER(OrcGeom), i, i, i, d, d, P, P, P]
+        _lib.orc_near_rule.restype = i
     return _lib
 
 
@@ -140,6 +143,27 @@ def integrate_element(dad, e, pf, source=-1, npg=20, nearfield="tanp3c", singula
                             1 if singular == "telles" else 0, e, float(pf[0]), float(pf[1]),
                             int(source), _p(h), _p(gg))
     return h, gg
+
+
+def cr_fn(name, x):
+    """Correctly rounded atan / tan / cbrt of the doubles x (quad precision
+    rounded once)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    lib().orc_cr_fn({"atan": 0, "tan": 1, "cbrt": 2}[name], _p(x), x.size, _p(out))
+    return out
+
+
+def near_rule(dad, e, pf, npg=16, nearfield="tanp3c"):
+    """Mapped nodes and weights of the near-field rule for element e and source
+    point pf, and the complex pole (z0, e0) they came from."""
+    g, keep = make_geom(dad)
+    eta = np.zeros(2 * npg + 2)
+    w = np.zeros(2 * npg + 2)
+    ze = np.zeros(2)
+    m = lib().orc_near_rule(ctypes.byref(g), npg, NEARFIELD[nearfield], int(e), float(pf[0]), float(pf[1]),
+                            _p(eta), _p(w), _p(ze))
+    return eta[:m], w[:m], ze
 
 
 def near_mask(dad, near_factor=1.5):

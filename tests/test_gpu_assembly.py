@@ -1,18 +1,18 @@
 """GPU parity of the assembly against the FP64 oracle, through the C ABI.
 
-Tolerances: FP64 path ||dM||/||M|| < 1e-10 (reference test/laplace.jl:414),
-FP32 path < 1e-6 (test/laplace.jl:454-455).
+Tolerances: FP64 path ||dM||/||M|| < 1e-10 (reference test/laplace.jl:414)
+and every entry within 1e-10 of the matrix's largest entry; FP32 path
+< 1e-6 (test/laplace.jl:454-455).
 
-The reference's near-singular tanp3c map is ill-conditioned when the
-complex pole of a neighbouring curved element sits just above its collinear
-cut-off (eta0 slightly above 1e-8, src/Core/Integration.jl:1165): there a
-1-ulp change of the source point moves the reference's own result by up to
-~3e-8 relative.  The FP64 bar is therefore max(1e-10, 10 x the oracle's own
-change when every coordinate is perturbed by 1 ulp) -- "identical within the
-reference algorithm's rounding sensitivity".  The perturbed oracle run keeps
-the unperturbed near/far split: regular meshes put points exactly on the
-near cut, where the split itself must match bit for bit (and does: the GPU's
-near test is IEEE round-to-nearest without contraction)."""
+The reference's near-singular tanp3c map amplifies rounding (a one-ulp
+change of an atan value or of the pole moves a neighbouring-element integral
+by up to ~5e-5 relative; tests/test_crmath_cpu.py measures it).  The GPU's
+map and the oracle's are the same IEEE operations with correctly rounded
+atan / tan / cbrt and Gauss rules, and tests/test_crmath_cpu.py checks their
+nodes and weights bit for bit; so the FP64 bar needs no allowance for that
+sensitivity.  Regular meshes put points exactly on the near cut (distance =
+1.5 L): the GPU's near test is IEEE round-to-nearest without contraction and
+resolves those ties as the reference does."""
 import numpy as np
 import pytest
 
@@ -43,12 +43,13 @@ def perturbed(dad, seed=0):
     return d.contiguous()
 
 
-def tol64(orc, dad, npg, Hr, Gr, **kw):
-    """FP64 bar: max(1e-10, 10 x the oracle's own 1-ulp sensitivity with the
-    near/far split held fixed)."""
-    m = orc.near_mask(dad, kw.get("near_factor", 1.5))
-    Hp, Gp = orc.assemble(perturbed(dad), npg=npg, store=False, mask=m, **kw)
-    return max(TOL64, 10 * rel(Hp, Hr)), max(TOL64, 10 * rel(Gp, Gr))
+def check64(M, Mr, what=""):
+    """FP64 bar: relative Frobenius error and every entry within 1e-10."""
+    M = np.asarray(M, np.float64)
+    e = rel(M, Mr)
+    d = float(np.max(np.abs(M - Mr))) / float(np.max(np.abs(Mr)))
+    assert e < TOL64 and d < TOL64, (what, e, d)
+    return e, d
 
 
 CASES = [
@@ -68,8 +69,8 @@ def test_laplace_hg_parity(orc, name, mk, npg):
     dad = mk()
     Hr, Gr = orc.assemble(dad, npg=npg, store=False)
     H, G = H_G_gpu(dad, T=np.float64, npg=npg, store=False)
-    th, tg = tol64(orc, dad, npg, Hr, Gr)
-    assert rel(H, Hr) < th and rel(G, Gr) < tg, (rel(H, Hr), th, rel(G, Gr), tg)
+    check64(H, Hr, "H")
+    check64(G, Gr, "G")
     H32, G32 = H_G_gpu(dad, T=np.float32, npg=npg, store=False)
     assert rel(H32, Hr) < TOL32 and rel(G32, Gr) < TOL32, (rel(H32, Hr), rel(G32, Gr))
     assert np.all(np.isfinite(H)) and np.all(np.isfinite(G32))
@@ -82,8 +83,8 @@ def test_geometry_from_nodes(orc):
     dad.geo = np.zeros((dad.ne, 0, 2))
     Hr, Gr = orc.assemble(dad, npg=16, store=False)
     H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
-    th, tg = tol64(orc, dad, 16, Hr, Gr)
-    assert rel(H, Hr) < th and rel(G, Gr) < tg
+    check64(H, Hr, "H")
+    check64(G, Gr, "G")
 
 
 def test_all_near(orc):
@@ -91,7 +92,8 @@ def test_all_near(orc):
     dad = quadrado(ndiv=6, pontointerno=True)
     Hr, Gr = orc.assemble(dad, npg=12, near_factor=np.inf, store=False)
     H, G = H_G_gpu(dad, T=np.float64, npg=12, near_factor=np.inf, store=False)
-    assert rel(H, Hr) < TOL64 and rel(G, Gr) < TOL64
+    check64(H, Hr, "H")
+    check64(G, Gr, "G")
 
 
 @pytest.mark.parametrize("ndiv", [5, 9])
@@ -99,8 +101,8 @@ def test_kelvin_hg_parity(orc, ndiv):
     dad = quadrado_elasticity(ndiv=ndiv, props=Elasticity(1.0, 0.3, 1.0), pontointerno=True)
     Hr, Gr = orc.assemble(dad, npg=12, store=False)
     H, G = H_G_gpu(dad, T=np.float64, npg=12, store=False)
-    th, tg = tol64(orc, dad, 12, Hr, Gr)
-    assert rel(H, Hr) < th and rel(G, Gr) < tg, (rel(H, Hr), rel(G, Gr))
+    check64(H, Hr, "H")
+    check64(G, Gr, "G")
     H32, G32 = H_G_gpu(dad, T=np.float32, npg=12, store=False)
     assert rel(H32, Hr) < TOL32 and rel(G32, Gr) < TOL32, (rel(H32, Hr), rel(G32, Gr))
 
@@ -112,8 +114,8 @@ def test_kelvin_curved_plane_stress(orc):
     dad.BV = np.zeros(2 * dad.n)
     Hr, Gr = orc.assemble(dad, npg=16, store=False)
     H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
-    th, tg = tol64(orc, dad, 16, Hr, Gr)
-    assert rel(H, Hr) < th and rel(G, Gr) < tg, (rel(H, Hr), th, rel(G, Gr), tg)
+    check64(H, Hr, "H")
+    check64(G, Gr, "G")
 
 
 @pytest.mark.parametrize("kind", ["laplace", "kelvin"])
@@ -127,11 +129,8 @@ def test_fused_system_matches_applybc(orc, kind):
     Hr, Gr = orc.assemble(dad, npg=16, store=False)
     Ar, br = orc.apply_bc(dad, Hr, Gr)
     A, b = assemble_system(dad, npg=16)
-    Hp, Gp = orc.assemble(perturbed(dad), npg=16, store=False, mask=orc.near_mask(dad))
-    Ap, bp = orc.apply_bc(dad, Hp, Gp)
-    ta, tb = max(TOL64, 10 * rel(Ap, Ar)), max(TOL64, 10 * rel(bp, br))
-    assert rel(A, Ar) < ta, (rel(A, Ar), ta)
-    assert rel(b, br) < tb, (rel(b, br), tb)
+    check64(A, Ar, "A")
+    assert rel(b, br) < TOL64, rel(b, br)
 
 
 @pytest.mark.parametrize("name,mk", [
@@ -172,8 +171,8 @@ def test_device_pointers_and_ld(orc):
     H = Hs.t()[: dad.nt]  # column-major view with ld
     G = Gs.t()[: dad.nt]
     H_G_gpu(dad, T=np.float64, npg=16, out=(H, G), store=False)
-    th, tg = tol64(orc, dad, 16, Hr, Gr)
-    assert rel(H.cpu().numpy(), Hr) < th and rel(G.cpu().numpy(), Gr) < tg
+    check64(H.cpu().numpy(), Hr, "H")
+    check64(G.cpu().numpy(), Gr, "G")
 
 
 def test_repeated_calls_reuse_workspace(orc):
@@ -182,8 +181,8 @@ def test_repeated_calls_reuse_workspace(orc):
     for dad in (a, b, a):
         Hr, Gr = orc.assemble(dad, npg=16, store=False)
         H, G = H_G_gpu(dad, T=np.float64, npg=16, store=False)
-        th, tg = tol64(orc, dad, 16, Hr, Gr)
-        assert rel(H, Hr) < th and rel(G, Gr) < tg
+        check64(H, Hr, "H")
+        check64(G, Gr, "G")
 
 
 def test_invalid_arguments_raise():
@@ -198,36 +197,24 @@ def test_invalid_arguments_raise():
         H_G_gpu(dad)
 
 
-def test_full_size_parity_within_reference_rounding_sensitivity(orc):
-    """At the full C2 size (2731 quadratic elements, N = 8193) the reference's
-    tanp3c map is ill-conditioned for points on the adjacent element (pole just
-    outside [-1, 1], nearly collinear): a 1-ulp change of the collocation point
-    moves such entries of the FP64 oracle itself by up to ~5e-5 relative.  Every
-    GPU entry that differs from the oracle by more than 1e-10 of the largest
-    entry must lie within 10x that spread, measured per pair on the oracle."""
+def test_full_size_parity_every_entry(orc):
+    """The full-size solve's matrices (2731 quadratic elements, N = 8193):
+    every entry of the FP64 H and G within 1e-10 of the largest entry, near
+    and on-element entries included (no rounding-sensitivity allowance)."""
     import os
     dad = star_domain(2731, p=2, seed=0)
     H, G = H_G_gpu(dad, T=np.float64, npg=16, near="gpu", store=False)
     Ho, Go = orc.assemble(dad, npg=16, threads=os.cpu_count() or 1, store=False)
-    pts = np.asarray(dad.collocation)
-    rng = np.random.default_rng(3)
-    for X, Y, which in ((H, Ho, 0), (G, Go, 1)):
-        D = np.abs(X - Y)
-        bar = 1e-10 * np.max(np.abs(Y))
-        rows, cols = np.nonzero(D > bar)
-        if which == 0:
-            # H_ii is the row sum: its difference is bounded by the row's
-            diag = rows == cols
-            for r in rows[diag]:
-                assert D[r, r] <= 1.0001 * (D[r].sum() - D[r, r]) + bar
-            rows, cols = rows[~diag], cols[~diag]
-        order = np.argsort(D[rows, cols])[::-1][:12]  # the largest differences
-        for r, c in zip(rows[order], cols[order]):
-            e = c // 3
-            assert np.min(np.linalg.norm(pts[3 * e:3 * e + 3] - pts[r], axis=1)) < 1.5 * dad.elem_length[e]
-            vals = [Y[r, c], orc.integrate_element(dad, e, pts[r].copy(), source=r, npg=16)[which][c - 3 * e]]
-            for _ in range(6):
-                pp = pts[r] * (1 + rng.choice([-1.0, 1.0], 2) * 2.0 ** -52)
-                vals.append(orc.integrate_element(dad, e, pp, source=r, npg=16)[which][c - 3 * e])
-            spread = max(vals) - min(vals)
-            assert D[r, c] <= 10 * spread + bar, (which, r, c, D[r, c], spread)
+    eh, dh = check64(H, Ho, "H")
+    eg, dg = check64(G, Go, "G")
+    # the near entries (neighbouring elements) on their own, relative to themselves
+    m = orc.near_mask(dad)
+    rows, els = np.nonzero(m)
+    cols = (3 * els[:, None] + np.arange(3)[None, :]).ravel()
+    rr = np.repeat(rows, 3)
+    off = rr != cols
+    gn = np.abs(G[rr, cols] - Go[rr, cols]) / np.abs(Go[rr, cols])
+    hn = np.abs(H[rr[off], cols[off]] - Ho[rr[off], cols[off]]) / np.abs(Ho[rr[off], cols[off]])
+    print(f"H: rel {eh:.2e} max entry {dh:.2e}; G: rel {eg:.2e} max entry {dg:.2e}; "
+          f"near entries max rel: G {gn.max():.2e}, H {hn.max():.2e}")
+    assert gn.max() < 1e-10
