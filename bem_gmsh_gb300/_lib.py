@@ -18,6 +18,9 @@ BEM_OPT_TCGEN05 = 1
 BEM_OPT_KERNEL_TIMING = 2
 BEM_OPT_FAR_DF = 3
 BEM_OPT_GRAPHS = 4
+BEM_OPT_PIVOT_FALLBACK = 5
+BEM_OPT_WAIT_LIMIT = 6
+BEM_OPT_INJECT = 7
 BEM_NOALLOC_MAX_NT, BEM_NOALLOC_MAX_NE = 16384, 8192
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
                   "lu_panels", "lu_thin"]
@@ -40,11 +43,15 @@ class BemGeom2D(ctypes.Structure):
 
 class BemSolveStats(ctypes.Structure):
     _fields_ = [("status", I32), ("iterations", I32), ("rel_residual", D), ("t_assemble_ms", D),
-                ("t_factor_ms", D), ("t_refine_ms", D)]
+                ("t_factor_ms", D), ("t_refine_ms", D), ("pivoted", I32), ("reserved", I32)]
 
 
 class BemError(RuntimeError):
-    pass
+    """A C-ABI call failed; `status` is its BEM_ERR_* code."""
+
+    def __init__(self, msg: str, status: int = 0):
+        super().__init__(msg)
+        self.status = status
 
 
 _lib = None
@@ -136,7 +143,7 @@ class Context:
     def check(self, rc: int, what: str):
         if rc != BEM_OK:
             msg = self.L.bem_last_error(self.h).decode()
-            raise BemError(f"{what}: {STATUS.get(rc, rc)} {msg}".strip())
+            raise BemError(f"{what}: {STATUS.get(rc, rc)} {msg}".strip(), rc)
 
     def set_option(self, option: int, value: int):
         self.check(self.L.bem_ctx_set_option(self.h, option, value), "set_option")

@@ -197,7 +197,8 @@ def solve(dad: BEMdata, npg: int = 20, mode: str = "mixed", tol: float = 1e-14, 
                            _lib.BEM_MEM_HOST, x.ctypes.data, st)
     ctx.check(rc, "solve")
     split_sol(dad, x)
-    stats = dict(iterations=st.iterations, rel_residual=st.rel_residual, t_assemble_ms=st.t_assemble_ms,
+    stats = dict(iterations=st.iterations, rel_residual=st.rel_residual, pivoted=bool(st.pivoted),
+                 t_assemble_ms=st.t_assemble_ms,
                  t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)
     dad.set_cache(solve_stats=stats)
     return (dad.T, stats) if return_stats else dad.T
@@ -223,7 +224,7 @@ def solve_system(A, b, mode: str = "mixed", tol: float = 1e-14, max_iter: int = 
                                 _ptr(x), st)
     ctx.check(rc, "solve_system")
     return x, dict(iterations=st.iterations, rel_residual=st.rel_residual,
-                   t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms)
+                   t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms, pivoted=bool(st.pivoted))
 
 
 def recover_strain_stress(dad: BEMdata, u=None, t=None, ctx: _lib.Context | None = None):

@@ -27,13 +27,14 @@ int ensure_workers(bem_ctx* c, int w) {
     bem_ctx* s = nullptr;
     int rc = bem_ctx_create(c->device, &s);
     if (rc != BEM_OK) return rc;
-    s->opt_tcgen05 = c->opt_tcgen05;
-    s->opt_far_df = c->opt_far_df;
     c->workers.push_back(s);
   }
   for (bem_ctx* s : c->workers) {
     s->opt_tcgen05 = c->opt_tcgen05;
     s->opt_far_df = c->opt_far_df;
+    s->opt_pivot_fallback = c->opt_pivot_fallback;
+    s->opt_wait_limit = c->opt_wait_limit;
+    s->opt_inject = c->opt_inject;
   }
   return BEM_OK;
 }

@@ -2,6 +2,7 @@
 // The entry points are declared (with the reference interfaces they replace)
 // in include/bem_gb300.h.
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -109,6 +110,7 @@ void bem_build_rules(const bem_geom2d* g, int npg, const double* ew_host, Rules&
 // context
 // ---------------------------------------------------------------------------
 void* bem_ctx::get(int slot, size_t bytes) {
+  if (opt_inject & 1) return nullptr;  // injected allocation failure (BEM_OPT_INJECT bit 0)
   Buf& b = slots[slot];
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) return b.p;
@@ -210,6 +212,8 @@ extern "C" int bem_ctx_create(int device, bem_ctx** out) {
   }
   bem_ctx* c = new bem_ctx();
   c->device = device;
+  // failure injection for tests (BEM_OPT_INJECT), from the environment
+  if (const char* inj = std::getenv("BEM_INJECT")) c->opt_inject = std::atoi(inj);
   cudaSetDevice(device);
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;

@@ -33,6 +33,12 @@ struct bem_ctx {
   int opt_tcgen05 = 1;  // BEM_OPT_TCGEN05: trailing updates on tcgen05
   int opt_far_df = 1;   // BEM_OPT_FAR_DF
   int opt_graphs = 1;   // BEM_OPT_GRAPHS
+  int opt_pivot_fallback = 1;      // BEM_OPT_PIVOT_FALLBACK
+  int opt_wait_limit = 1 << 20;    // BEM_OPT_WAIT_LIMIT
+  int opt_inject = 0;              // BEM_OPT_INJECT
+  // why the last mixed solve did not converge (MIXED_*)
+  enum { MIXED_OK = 0, MIXED_PIVOT = 1, MIXED_STAGNATION = 2, MIXED_CAP = 3 };
+  int mixed_fail = MIXED_OK;
   // captured factorization of the mixed solve, replayed while the buffers and
   // sizes in its key are unchanged (captured on the second call with a key)
   cudaGraphExec_t lu_graph = nullptr;

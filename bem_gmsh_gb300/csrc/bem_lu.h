@@ -30,9 +30,13 @@ void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float
 // out <- U^{-1} L^{-1} r on padded FP32 vectors.  tmp: Npad floats (the
 // forward result); tags: 2 Npad words of (epoch, value) scratch, zeroed
 // before the first call; epoch: > 0 and different in every call on the same
-// tags; err: timeout flag.  r may be clobbered.  Returns 0 or a CUDA error.
+// tags; err: timeout flag, set when a wait polled wait_limit times in vain.
+// wepoch_shift (failure injection, normally 0): results are published under
+// epoch + wepoch_shift, so that a nonzero shift makes every dependent wait
+// run out.  r may be clobbered.  Returns 0 or a CUDA error.
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
-                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st);
+                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st,
+                 int wait_limit = 1 << 20, int wepoch_shift = 0);
 
 void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
                 cudaStream_t st);

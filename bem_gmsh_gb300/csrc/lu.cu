@@ -539,7 +539,7 @@ template <bool UPPER>
 __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, int64_t ld, int K,
                                                    const float* __restrict__ Dinv, const float* __restrict__ Mc,
                                                    const float* r, float* y, unsigned long long* tags, int epoch,
-                                                   int* err) {
+                                                   int wepoch, int wait_limit, int* err) {
   extern __shared__ float Ds[];  // the block's inverse, [col][row], LU_NB * (LU_NB + 1)
   __shared__ float ys[LU_NB];
   __shared__ float part[2][LU_NB];
@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
       unsigned long long v = ld_acquire_u64(w);
       int it = 0;
       while ((int)(v >> 32) != epoch) {
-        if (++it > (1 << 20)) {
+        if (++it > wait_limit) {
           bad = 1;
           break;
         }
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
   }
   if (t < LU_NB) {
     y[rb + t] = yb;
-    st_relaxed_u64(tags + rb + t, ((unsigned long long)(unsigned)epoch << 32) | __float_as_uint(yb));
+    st_relaxed_u64(tags + rb + t, ((unsigned long long)(unsigned)wepoch << 32) | __float_as_uint(yb));
   }
 }
 
@@ -1568,7 +1568,9 @@ void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float
 }
 
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
-                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st) {
+                 float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st, int wait_limit,
+                 int wepoch_shift) {
+  const int wepoch = epoch + wepoch_shift;
   const int K = Npad / LU_NB;
   static int max_coresident = 0;
   static std::once_flag once;
@@ -1594,7 +1596,7 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const 
   unsigned long long* t1 = tags + Npad;
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&r, (void*)&tmp,
-                    (void*)&t0, (void*)&epoch, (void*)&err};
+                    (void*)&t0, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit, (void*)&err};
     // forward: r -> tmp (separate output so that no CTA reads a block another rewrote)
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, dim3(K), dim3(256), args,
                                                 dsm, st);
@@ -1602,7 +1604,7 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const 
   }
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&tmp, (void*)&out,
-                    (void*)&t1, (void*)&epoch, (void*)&err};
+                    (void*)&t1, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit, (void*)&err};
     cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, dim3(K), dim3(256), args,
                                                 dsm, st);
     if (e != cudaSuccess) return (int)e;

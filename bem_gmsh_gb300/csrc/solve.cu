@@ -140,6 +140,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   const int K = Npad / LU_NB;
   const int m = 30;  // restart length
   cudaStream_t st = c->stream;
+  c->mixed_fail = bem_ctx::MIXED_OK;
   float* A32 = (float*)c->get(bem_ctx::SLOT_LU0, sizeof(float) * (size_t)Npad * Npad);
   double* cs = (double*)c->get(bem_ctx::SLOT_LU1, sizeof(double) * (size_t)N);
   float* Dinv = (float*)c->get(bem_ctx::SLOT_LU2, sizeof(float) * bem::lu_dinv_floats(K));
@@ -251,13 +252,15 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   }
   if (hinfo != 0) {
     c->last_error = "vanishing pivot in block " + std::to_string(hinfo - 1) + " of the LU";
+    c->mixed_fail = bem_ctx::MIXED_PIVOT;
     if (stats) stats->status = BEM_ERR_NOT_CONVERGED;
     return BEM_ERR_NOT_CONVERGED;
   }
   int prc = 0;
   auto precond = [&](const double* v, double* z) {
     bem::to_f32(v, N, Npad, rf, st);
-    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, Mc, rf, tmpf, outf, tags, ++epoch, werr, st);
+    int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, Mc, rf, tmpf, outf, tags, ++epoch, werr, st,
+                               c->opt_wait_limit, (c->opt_inject & 2) ? 1 : 0);
     if (e2) prc = e2;
     bem::from_f32_scale(outf, cs, N, z, st);
   };
@@ -285,10 +288,18 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
     double beta = std::sqrt(dev_dot(c, w, w, N, hbuf, pin.dot));
     relres = beta / bnorm;
     if (relres <= tol) { converged = true; break; }
-    // stagnation at the FP64 rounding floor (a tol below eps |A| |x| / |b|
-    // cannot be reached): a restart cycle that no longer halves the true
-    // residual ends the refinement
-    if (relres < 1e-10 && beta > 0.5 * prev_beta) break;
+    if (beta > 0.5 * prev_beta) {
+      // a restart cycle that no longer halves the true residual.  Below 1e-10
+      // this is the FP64 rounding floor of the matrix (about eps |A| |x| / |b|;
+      // a tol below it cannot be reached): x is then backward stable, as
+      // accurate as FP64 allows -- what the reference's LU returns -- and
+      // counts as converged (stats report the residual reached).
+      if (relres < 1e-10) { converged = true; break; }
+      // far above that floor the same stall means the unpivoted FP32 factors
+      // are no preconditioner for this matrix (pivot growth)
+      c->mixed_fail = bem_ctx::MIXED_STAGNATION;
+      break;
+    }
     prev_beta = beta;
     bem::scale_copy64(w, 1.0 / beta, V, N, st);
     std::fill(gvec.begin(), gvec.end(), 0.0);
@@ -363,7 +374,12 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
     stats->t_refine_ms = tr.ms();
   }
   if (!converged) {
-    c->last_error = "GMRES refinement reached its iteration cap";
+    if (c->mixed_fail == bem_ctx::MIXED_STAGNATION) {
+      c->last_error = "GMRES refinement stagnated (the unpivoted LU is no preconditioner for this matrix)";
+    } else {
+      c->mixed_fail = bem_ctx::MIXED_CAP;
+      c->last_error = "GMRES refinement reached its iteration cap";
+    }
     return BEM_ERR_NOT_CONVERGED;
   }
   return BEM_OK;
@@ -417,6 +433,40 @@ int bem_solve_fp64_dev(bem_ctx* c, int N, double* A64, int64_t lda, const double
   return BEM_OK;
 }
 
+// The mixed solve with its pivoting safety net (BEM_OPT_PIVOT_FALLBACK).
+// The reference factors with partial pivoting (LAPACK getrf behind
+// `bem_linsolve`, src/Core/LinearSolveUtils.jl:44-49); the FP32 LU here does
+// not pivot, which BEM collocation systems (column-equilibrated) never need
+// but an arbitrary matrix can.  When that LU meets a vanishing pivot, or the
+// refinement stagnates far above the FP64 rounding floor, the system is
+// solved again by LU with partial pivoting in FP64.  A64 is factored in
+// place when `a_scratch` (the caller's copy), otherwise a copy is.
+int bem_solve_mixed_safe(bem_ctx* c, int N, double* A64, int64_t lda, bool a_scratch, const double* b,
+                         double tol, int max_iter, double* x, bem_solve_stats* stats) {
+  int rc = bem_solve_mixed_dev(c, N, A64, lda, b, tol, max_iter, 1, x, stats);
+  if (rc != BEM_ERR_NOT_CONVERGED || !c->opt_pivot_fallback) return rc;
+  if (c->mixed_fail != bem_ctx::MIXED_PIVOT && c->mixed_fail != bem_ctx::MIXED_STAGNATION) return rc;
+  double* Af = A64;
+  int64_t ldf = lda;
+  if (!a_scratch) {
+    Af = (double*)c->get(bem_ctx::SLOT_OUT2, sizeof(double) * (size_t)N * N);
+    if (!Af) return BEM_ERR_NOMEM;
+    cudaMemcpy2DAsync(Af, sizeof(double) * N, A64, sizeof(double) * lda, sizeof(double) * N, N,
+                      cudaMemcpyDeviceToDevice, c->stream);
+    ldf = N;
+  }
+  bem_solve_stats st2{};
+  int rc2 = bem_solve_fp64_dev(c, N, Af, ldf, b, x, &st2);
+  if (stats) {
+    stats->pivoted = 1;
+    stats->status = st2.status;
+    stats->rel_residual = NAN;
+    stats->t_factor_ms += st2.t_factor_ms;
+    stats->t_refine_ms += st2.t_refine_ms;
+  }
+  return rc2;
+}
+
 extern "C" int bem_solve_system(bem_ctx* c, int64_t n, const double* A, int64_t lda, const double* b,
                                 int mode, double tol, int max_iter, int mem, double* x,
                                 bem_solve_stats* stats) {
@@ -450,7 +500,7 @@ extern "C" int bem_solve_system(bem_ctx* c, int64_t n, const double* A, int64_t 
     dx = tmp + N;
   }
   int rc = mode == BEM_SOLVE_MIXED
-               ? bem_solve_mixed_dev(c, N, dA, ldd, db, tol, max_iter, 1, dx, stats)
+               ? bem_solve_mixed_safe(c, N, (double*)dA, ldd, Acopy != nullptr, db, tol, max_iter, dx, stats)
                : bem_solve_fp64_dev(c, N, (double*)dA, ldd, db, dx, stats);
   if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;
   if (mem == BEM_MEM_HOST) {
@@ -501,7 +551,7 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   ta.stop(c->stream);
   if (rc) return rc;
   double t_asm = ta.ms();
-  rc = mode == BEM_SOLVE_MIXED ? bem_solve_mixed_dev(c, N, A, ld, b, tol, max_iter, 1, dx, stats)
+  rc = mode == BEM_SOLVE_MIXED ? bem_solve_mixed_safe(c, N, A, ld, true, b, tol, max_iter, dx, stats)
                                : bem_solve_fp64_dev(c, N, A, ld, b, dx, stats);
   if (stats) stats->t_assemble_ms = t_asm;
   if (rc != BEM_OK && rc != BEM_ERR_NOT_CONVERGED) return rc;
@@ -536,6 +586,20 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   }
   if (option == BEM_OPT_GRAPHS) {
     c->opt_graphs = value ? 1 : 0;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_PIVOT_FALLBACK) {
+    c->opt_pivot_fallback = value ? 1 : 0;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_WAIT_LIMIT) {
+    if (value < 1) return BEM_ERR_INVALID;
+    c->opt_wait_limit = value;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_INJECT) {
+    if (value < 0 || value > 3) return BEM_ERR_INVALID;
+    c->opt_inject = value;
     return BEM_OK;
   }
   return BEM_ERR_INVALID;

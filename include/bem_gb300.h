@@ -54,6 +54,21 @@ extern "C" {
                                    LU, sweep couplings) is captured in a CUDA graph on the second call with
                                    unchanged buffers and replayed; 0: direct launches.  Not used while
                                    BEM_OPT_KERNEL_TIMING is on. */
+#define BEM_OPT_PIVOT_FALLBACK 5 /* 1 (default): a mixed solve whose FP32 LU (no pivoting) meets a
+                                   vanishing pivot, or whose refinement stagnates above the FP64
+                                   rounding floor (a restart cycle that does not halve the residual),
+                                   is solved again by LU with partial pivoting in FP64 (the LAPACK
+                                   getrf semantics of `bem_linsolve`), stats->pivoted = 1; 0: such a
+                                   solve returns BEM_ERR_NOT_CONVERGED.  Reaching max_iter alone
+                                   always returns BEM_ERR_NOT_CONVERGED. */
+#define BEM_OPT_WAIT_LIMIT 6    /* polls before a device-side wait of the triangular sweeps gives up
+                                   and the call returns BEM_ERR_INTERNAL (default 1 << 20, >= 1) */
+#define BEM_OPT_INJECT 7        /* failure injection for tests, host side (default 0, or the value of
+                                   the environment variable BEM_INJECT when the context is created):
+                                   bit 0: every workspace allocation fails (BEM_ERR_NOMEM); bit 1: the
+                                   triangular sweeps publish their results under another epoch than
+                                   the one their readers wait for, so those bounded waits run out
+                                   (BEM_ERR_INTERNAL, the context stays usable) */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */
@@ -107,6 +122,10 @@ typedef struct bem_solve_stats {
   double t_assemble_ms;  /* device time of the assembly */
   double t_factor_ms;    /* device time of the LU */
   double t_refine_ms;    /* device time of the refinement */
+  int32_t pivoted;       /* 1: the mixed solve's unpivoted factorization broke down (vanishing
+                            pivot) or its refinement stagnated, and the system was solved by LU
+                            with partial pivoting in FP64 (BEM_OPT_PIVOT_FALLBACK) */
+  int32_t reserved;
 } bem_solve_stats;
 
 /* Context: one device, one stream, cached device workspace.  Replaces the
@@ -163,9 +182,15 @@ int bem_assemble_system2d(bem_ctx* ctx, const bem_geom2d* geom, int kind, double
  *   BEM_SOLVE_MIXED: columns equilibrated, FP32 copy factored by a blocked
  *     LU without pivoting whose updates run on TF32 tensor cores (3xTF32
  *     split), then FP64 restarted GMRES on the FP64 matrix, preconditioned
- *     by that LU, until ||b - A x|| <= tol ||b|| or max_iter iterations
- *     (then BEM_ERR_NOT_CONVERGED with x the last iterate).  A is not
- *     modified.
+ *     by that LU, until ||b - A x|| <= tol ||b||, or until a restart cycle no
+ *     longer halves a residual below 1e-10 ||b|| (the FP64 rounding floor of
+ *     the matrix: x is backward stable, like the reference's LU solution;
+ *     stats->rel_residual reports the residual reached), or max_iter
+ *     iterations (then BEM_ERR_NOT_CONVERGED with x the last iterate).  A
+ *     vanishing pivot of the unpivoted LU, or a refinement that stalls
+ *     above that floor, hands the system to LU with partial pivoting in
+ *     FP64 (BEM_OPT_PIVOT_FALLBACK, on by default; stats->pivoted = 1).  A is
+ *     not modified.
  *   BEM_SOLVE_FP64: LU with partial pivoting in FP64 (cuSOLVER getrf/getrs,
  *     the FP64 comparison path).
  * stats may be NULL.
