@@ -17,7 +17,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .geometry import BEMdata, Laplace, Elasticity
+from .geometry import BEMdata, Laplace, Elasticity, from_nodes
 
 _KEEP = "_bem_keepalive"
 
@@ -427,6 +427,32 @@ def adjoint_laplace(dad: BEMdata, q_target, npg: int = 16, near_factor: float = 
         return out + (dict(status=st.status, iterations=st.iterations, t_assemble_ms=st.t_assemble_ms,
                            t_factor_ms=st.t_factor_ms, t_refine_ms=st.t_refine_ms),)
     return out
+
+
+def shape_misfit(X, p: int, BC, BV, q_target, npg: int = 16, ctx: _lib.Context | None = None) -> float:
+    """J(X) = 1/2 sum_{BC=0} (q_i - q_target_i)^2 for boundary nodes X (n, 2)
+    of elements that interpolate their own p+1 nodes (element e owns rows
+    e(p+1) .. e(p+1)+p), BC, BV and q_target fixed.  The primal of the
+    ChainRulesCore `rrule` that INTEGRATION.md gives for Julia."""
+    return shape_misfit_rrule(X, p, BC, BV, q_target, npg=npg, ctx=ctx)[0]
+
+
+def shape_misfit_rrule(X, p: int, BC, BV, q_target, npg: int = 16, ctx: _lib.Context | None = None):
+    """(J, pullback) with pullback(dJ) = dJ * dJ/dX, (n, 2): the call sequence
+    of the Julia `rrule` -- one bem_adjoint_laplace2d call (forward solve,
+    adjoint solve, backward kernels) for the value and the gradient, and a
+    pullback that only scales the stored gradient by the incoming cotangent."""
+    X = np.asarray(X, dtype=np.float64)
+    n = X.shape[0]
+    if X.shape != (n, 2) or n % (p + 1):
+        raise ValueError("X must be (n, 2) with n a multiple of p + 1")
+    dad = from_nodes("shape", X.reshape(n // (p + 1), p + 1, 2), p, Laplace(1.0), BC, BV)
+    J, grad = adjoint_laplace(dad, q_target, npg=npg, ctx=ctx)
+
+    def pullback(dJ):
+        return float(dJ) * grad
+
+    return J, pullback
 
 
 def adjoint_laplace_batch(cases, npg: int = 16, near_factor: float = 1.5, tol: float = 1e-14,

@@ -88,3 +88,31 @@ def test_adjoint_batch_matches_single_calls():
         # same kernels per domain; row sums use FP64 atomics, so agree to rounding
         assert abs(J - J1) <= 1e-10 * max(abs(J1), 1e-300)
         assert np.linalg.norm(g - g1) <= 1e-9 * np.linalg.norm(g1)
+
+
+def test_rrule_call_sequence(orc):
+    """The call sequence of the Julia ChainRulesCore rrule,
+    through its Python mirror: the primal equals the rrule's value, the
+    pullback scales the gradient by the incoming cotangent, and a tangent V
+    contracted with the pullback's output -- what reverse-mode AD does for
+    theta -> J(X0 + theta V) -- matches central differences (h = 1e-6) of
+    the FP64 oracle."""
+    from bem_gmsh_gb300.api import shape_misfit, shape_misfit_rrule
+    dad, target = star_adjoint_case(20, p=2, seed=7)
+    qt = target_q(orc, target)
+    X0 = np.asarray(dad.collocation).copy()
+    J, pb = shape_misfit_rrule(X0, 2, dad.BC, dad.BV, qt)
+    # the same value as the primal (to rounding: the row sums are FP64 atomics)
+    assert abs(J - shape_misfit(X0, 2, dad.BC, dad.BV, qt)) <= 1e-12 * J
+    g1 = pb(1.0)
+    assert g1.shape == X0.shape
+    assert np.array_equal(pb(2.5), 2.5 * g1)
+    # a smooth tangent: radial bulge cos(3 theta)
+    th = np.arctan2(X0[:, 1], X0[:, 0])
+    V = (np.cos(3 * th))[:, None] * X0 / np.linalg.norm(X0, axis=1)[:, None]
+    dJ = float(np.sum(g1 * V))
+    h = 1e-6
+    Jp = oracle_J(orc, (X0 + h * V).reshape(dad.ne, 3, 2), 2, dad.BC, dad.BV, qt, 16)
+    Jm = oracle_J(orc, (X0 - h * V).reshape(dad.ne, 3, 2), 2, dad.BC, dad.BV, qt, 16)
+    fd = (Jp - Jm) / (2 * h)
+    assert abs(dJ - fd) <= 1e-5 * abs(fd), (dJ, fd)
