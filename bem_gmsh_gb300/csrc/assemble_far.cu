@@ -102,6 +102,36 @@ __global__ void pack_nodes_df_kernel(GeomDev g, Rules R, Physics ph, const doubl
   nodes[j] = r;
 }
 
+// double-float node record (Kelvin): the constants of kelvin_UT times J w,
+// cU = J w / (2 prod1 mu), cUl = -(3 - 4 nu) / 2 cU (the log(1/R) term as
+// log(R2)), cT = -J w / prod1 with prod1 = 4 pi (1 - nu), and the node's two
+// boundary values
+__global__ void pack_nodes_dfk_kernel(GeomDev g, Rules R, Physics ph, const double* bv, NodeDFK* nodes) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= g.n) return;
+  NodeDFK r;
+  df::split3(g.px[j], r.xa, r.xb, r.xc);
+  df::split3(g.py[j], r.ya, r.yb, r.yc);
+  df::f2 t = df::from_double(g.nx[j]);
+  r.nxh = t.h; r.nxl = t.l;
+  t = df::from_double(g.ny[j]);
+  r.nyh = t.h; r.nyl = t.l;
+  const double wjk = g.jac[j] * R.ew[j % g.nn];
+  const double prod1 = 4 * kPi * (1 - ph.nu);
+  const double cU = wjk / (2 * prod1 * ph.mu);
+  t = df::from_double(cU);
+  r.cUh = t.h; r.cUl = t.l;
+  t = df::from_double(-(3 - 4 * ph.nu) / 2 * cU);
+  r.cLh = t.h; r.cLl = t.l;
+  t = df::from_double(-wjk / prod1);
+  r.cTh = t.h; r.cTl = t.l;
+  t = df::from_double(bv ? bv[2 * j] : 0.0);
+  r.bv0h = t.h; r.bv0l = t.l;
+  t = df::from_double(bv ? bv[2 * j + 1] : 0.0);
+  r.bv1h = t.h; r.bv1l = t.l;
+  nodes[j] = r;
+}
+
 // element record (32 B): conservative box of the element's nodes and the
 // squared near limit, widened so that a pair the box test calls far is far
 // for the exact FP64 test as well.
@@ -300,13 +330,15 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
   constexpr int BE = 32;                   // elements per tile
   const int nn = a.nn;
 
-  constexpr int NDB = (PREC == 3) ? (int)sizeof(NodeDF) : (int)sizeof(NodeRec);
+  constexpr int NDB =
+      (PREC == 3) ? (NC == 1 ? (int)sizeof(NodeDF) : (int)sizeof(NodeDFK)) : (int)sizeof(NodeRec);
   __shared__ __align__(16) ElemRec s_el[BE];
   __shared__ __align__(16) unsigned char s_ndraw[BE * BEM_MAXNN * NDB];
   __shared__ __align__(16) float4 s_log[PREC == 3 ? df::kLogTable : 1];
   __shared__ __align__(8) uint64_t s_bar;
   const NodeRec* s_nd = (const NodeRec*)s_ndraw;
   const NodeDF* s_ndf = (const NodeDF*)s_ndraw;
+  const NodeDFK* s_ndk = (const NodeDFK*)s_ndraw;
   __shared__ double s_red[EL][32 * SPT * DOF * DOF];
   __shared__ double s_redb[EL][32 * SPT * DOF];
 
@@ -332,7 +364,7 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
     mbar_expect_tx(&s_bar, eb + nb);
     bulk_g2s(s_el, a.elems + e0, eb, &s_bar);
     if constexpr (PREC == 3)
-      bulk_g2s(s_ndraw, a.nodes_df + (size_t)e0 * nn, nb, &s_bar);
+      bulk_g2s(s_ndraw, (const unsigned char*)a.nodes_df + (size_t)e0 * nn * NDB, nb, &s_bar);
     else
       bulk_g2s(s_ndraw, a.nodes + (size_t)e0 * nn, nb, &s_bar);
   }
@@ -362,15 +394,17 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
   }
   // double-float state: three-float source coordinates, row sums and b
   float s3x[PREC == 3 ? SPT : 1][3], s3y[PREC == 3 ? SPT : 1][3];
-  df::f2 rs_df[PREC == 3 ? SPT : 1], b_df[PREC == 3 ? SPT : 1];
+  df::f2 rs_df[PREC == 3 ? SPT * DOF * DOF : 1], b_df[PREC == 3 ? SPT * DOF : 1];
   if constexpr (PREC == 3) {
 #pragma unroll
     for (int s = 0; s < SPT; ++s) {
       df::split3(sx[s], s3x[s][0], s3x[s][1], s3x[s][2]);
       df::split3(sy[s], s3y[s][0], s3y[s][1], s3y[s][2]);
-      rs_df[s] = df::f2{0.f, 0.f};
-      b_df[s] = df::f2{0.f, 0.f};
     }
+#pragma unroll
+    for (int r = 0; r < SPT * DOF * DOF; ++r) rs_df[r] = df::f2{0.f, 0.f};
+#pragma unroll
+    for (int r = 0; r < SPT * DOF; ++r) b_df[r] = df::f2{0.f, 0.f};
   }
 
   double rowsum[SPT * DOF][DOF];  // [row][column dof]
@@ -394,8 +428,71 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
     bool far[SPT];
 #pragma unroll
     for (int s = 0; s < SPT; ++s) far[s] = box_far(sxh[s], sxl[s], syh[s], syl[s], E) || !valid[s];
-    if constexpr (PREC == 3) {
-      static_assert(NC == 1 && FUSED, "double-float far field: fused Laplace only");
+    if constexpr (PREC == 3 && NC == 4) {
+      static_assert(FUSED && SPT == 1, "double-float Kelvin far field: fused, one source point per thread");
+      const df::LogEntry* tab = (const df::LogEntry*)s_log;
+      const df::f2 cc{a.c1h, a.c1l};
+      for (int k = 0; k < nn; ++k) {
+        const NodeDFK nd = s_ndk[el * nn + k];
+        const int j = e * nn + k;
+        df::f2 U[4], T[4];
+        if (far[0]) {
+          const df::f2 rx = df::diff3(nd.xa, nd.xb, nd.xc, s3x[0][0], s3x[0][1], s3x[0][2]);
+          const df::f2 ry = df::diff3(nd.ya, nd.yb, nd.yc, s3y[0][0], s3y[0][1], s3y[0][2]);
+          const df::f2 R2 = df::add(df::sqr(rx), df::sqr(ry));
+          const df::f2 inv = df::div(df::f2{1.f, 0.f}, R2);
+          const df::f2 lg = df::log(R2, tab);
+          const df::f2 nxd{nd.nxh, nd.nxl}, nyd{nd.nyh, nd.nyl};
+          const df::f2 cU{nd.cUh, nd.cUl}, cL{nd.cLh, nd.cLl}, cT{nd.cTh, nd.cTl};
+          const df::f2 qxx = df::mul(df::sqr(rx), inv), qyy = df::mul(df::sqr(ry), inv);
+          const df::f2 qxy = df::mul(df::mul(rx, ry), inv);
+          const df::f2 rn = df::add(df::mul(rx, nxd), df::mul(ry, nyd));
+          const df::f2 ul = df::mul(cL, lg);
+          U[0] = df::add(ul, df::mul(cU, qxx));
+          U[1] = df::mul(cU, qxy);
+          U[2] = U[1];
+          U[3] = df::add(ul, df::mul(cU, qyy));
+          const df::f2 sT = df::mul(cT, df::mul(rn, inv));
+          T[0] = df::mul(sT, df::add(cc, df::add(qxx, qxx)));
+          T[3] = df::mul(sT, df::add(cc, df::add(qyy, qyy)));
+          const df::f2 cti = df::mul(cT, inv);
+          const df::f2 t2 = df::mul(df::add(rn, rn), qxy);
+          const df::f2 tw = df::mul(cc, df::add(df::mul(rx, nyd), df::neg(df::mul(ry, nxd))));
+          T[1] = df::mul(cti, df::add(t2, df::neg(tw)));
+          T[2] = df::mul(cti, df::add(t2, tw));
+        } else {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) U[c] = T[c] = df::f2{0.f, 0.f};
+        }
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          const int col = 2 * j + b;
+          const bool gcol = a.bc[col] == 0;  // column takes -G and b takes -H bv
+          const df::f2 bvv = b == 0 ? df::f2{nd.bv0h, nd.bv0l} : df::f2{nd.bv1h, nd.bv1l};
+          const df::f2 bvs = gcol ? df::neg(bvv) : bvv;
+          double av[2];
+#pragma unroll
+          for (int ar = 0; ar < 2; ++ar) {
+            const df::f2 Tv = T[ar * 2 + b], Uv = U[ar * 2 + b];
+            rs_df[ar * 2 + b] = df::add(rs_df[ar * 2 + b], Tv);
+            b_df[ar] = df::add(b_df[ar], df::mul(gcol ? Tv : Uv, bvs));
+            av[ar] = df::to_double(gcol ? df::neg(Uv) : Tv);
+          }
+          if (far[0] && valid[0]) {
+            double* Ac = (double*)a.H + (size_t)src0 * 2 + (size_t)col * ld;
+            if (vec_ok) {
+              *(double2*)Ac = make_double2(av[0], av[1]);
+            } else {
+              Ac[0] = av[0];
+              Ac[1] = av[1];
+            }
+          }
+        }
+      }
+      continue;
+    }
+    if constexpr (PREC == 3 && NC == 1) {
+      static_assert(FUSED, "double-float far field: fused systems only");
       const df::LogEntry* tab = (const df::LogEntry*)s_log;
       for (int k = 0; k < nn; ++k) {
         const NodeDF nd = s_ndf[el * nn + k];
@@ -534,9 +631,11 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
   }
   if constexpr (PREC == 3) {
 #pragma unroll
-    for (int s = 0; s < SPT; ++s) {
-      rowsum[s][0] = (double)rs_df[s].h + (double)rs_df[s].l;
-      bacc[s] = (double)b_df[s].h + (double)b_df[s].l;
+    for (int r = 0; r < SPT * DOF; ++r) {
+#pragma unroll
+      for (int b = 0; b < DOF; ++b)
+        rowsum[r][b] = (double)rs_df[r * DOF + b].h + (double)rs_df[r * DOF + b].l;
+      bacc[r] = (double)b_df[r].h + (double)b_df[r].l;
     }
   }
   // reduce row sums across element lanes, one FP64 atomic per row
@@ -591,7 +690,14 @@ static void launch_variant(const AsmRequest& q, cudaStream_t st) {
   fa.nodes_df = q.nodes_df; fa.logtab = q.logtab;
   if constexpr (PREC == 3) {
     logtab_kernel<<<1, 160, 0, st>>>(q.logtab);
-    pack_nodes_df_kernel<<<(g.n + 255) / 256, 256, 0, st>>>(g, q.R, q.ph, q.bv, q.nodes_df);
+    if constexpr (NC == 1) {
+      pack_nodes_df_kernel<<<(g.n + 255) / 256, 256, 0, st>>>(g, q.R, q.ph, q.bv, q.nodes_df);
+    } else {
+      pack_nodes_dfk_kernel<<<(g.n + 255) / 256, 256, 0, st>>>(g, q.R, q.ph, q.bv, (NodeDFK*)q.nodes_df);
+      const df::f2 c1 = df::from_double(1 - 2 * q.ph.nu);
+      fa.c1h = c1.h;
+      fa.c1l = c1.l;
+    }
     count_launches(2);
   }
   fa.px = g.px; fa.py = g.py; fa.nx = g.nx; fa.ny = g.ny; fa.jac = g.jac;
@@ -688,6 +794,7 @@ int launch_assembly(const AsmRequest& q, cudaStream_t st) {
     case 110: launch_variant<4, 1, false>(q, st); break;
     case 111: launch_variant<4, 1, true>(q, st); break;
     case 121: launch_variant<4, 2, true>(q, st); break;
+    case 131: launch_variant<4, 3, true>(q, st); break;
     default: return (int)cudaErrorInvalidValue;
   }
   return (int)cudaGetLastError();

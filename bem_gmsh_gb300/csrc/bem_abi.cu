@@ -386,7 +386,8 @@ int bem_run_assembly(bem_ctx* c, AsmRequest& q) {
   q.ev_join = c->asm_join;
   q.ev_join2 = c->asm_join2;
   if (q.prec == 3) {
-    q.nodes_df = (bem::NodeDF*)c->get(bem_ctx::SLOT_NODES_DF, sizeof(bem::NodeDF) * (size_t)q.g.n);
+    const size_t rec = q.ph.kind == 0 ? sizeof(bem::NodeDF) : sizeof(bem::NodeDFK);
+    q.nodes_df = (bem::NodeDF*)c->get(bem_ctx::SLOT_NODES_DF, rec * (size_t)q.g.n);
     q.logtab = (float4*)c->get(bem_ctx::SLOT_LOGTAB, sizeof(float4) * 136);
     if (!q.nodes_df || !q.logtab) return BEM_ERR_NOMEM;
   }
@@ -529,7 +530,7 @@ extern "C" int bem_assemble_system2d(bem_ctx* c, const bem_geom2d* g, int kind, 
   const int dof = kind == 0 ? 1 : 2;
   const int64_t rows = (int64_t)dof * g->nt;
   if (lda < rows) return BEM_ERR_INVALID;
-  const int prec = (kind == 0 && c->opt_far_df >= 2) ? 3 : 1;
+  const int prec = c->opt_far_df >= 2 ? 3 : 1;
   if (mem == BEM_MEM_DEVICE)
     return bem_assemble_system_dev(c, g, ph, BC, BV, npg, nf, mem, prec, A, lda, nullptr, b);
   const int64_t ldp = (rows + 3) / 4 * 4;

@@ -24,6 +24,20 @@ struct __align__(16) NodeDF {
   float bvh, bvl;
 };
 
+// 80-byte node record of the double-float far field (Kelvin): coordinates
+// as exact three-float splits; normal, the folded kernel constants and the
+// two boundary values as hi + lo pairs.  With q = r r^T / R2 and the node's
+// J w folded in:  U = cUl log(R2) I + cU q,
+//   T_aa = cT (r.n) / R2 (c + 2 q_aa),
+//   T_ab = cT / R2 (2 (r.n) q_ab - c (r_a n_b - r_b n_a)),
+// c = 1 - 2 nu (a kernel argument), the 2x2 Kelvin blocks of kelvin_UT.
+struct __align__(16) NodeDFK {
+  float xa, xb, xc, ya, yb, yc;
+  float nxh, nxl, nyh, nyl;
+  float cUh, cUl, cLh, cLl, cTh, cTl;
+  float bv0h, bv0l, bv1h, bv1l;
+};
+
 // 32-byte element record: conservative bounding box + squared near limit.
 struct __align__(16) ElemRec {
   float lox, loy, hix, hiy;
@@ -37,7 +51,8 @@ struct FarArgs {
   Physics ph;
   const float4* rows;
   const NodeRec* nodes;
-  const NodeDF* nodes_df;   // double-float variant only
+  const NodeDF* nodes_df;   // double-float variant only (Kelvin: NodeDFK records)
+  float c1h, c1l;           // double-float Kelvin: c = 1 - 2 nu as hi + lo
   const float4* logtab;     // double-float log table (129 entries)
   const ElemRec* elems;
   const double *px, *py, *nx, *ny, *jac;
@@ -99,7 +114,7 @@ struct AsmRequest {
   Physics ph;
   double near_factor;
   int prec;    // 0 FP32, 1 FP64, 2 FP64 + FP32 copy of A, 3 FP64 output with the
-               // far field in double-float (Laplace, fused)
+               // far field in double-float (fused)
   int fused;   // 1: write A, b (applyBC fused), else H, G
   void* H;
   int64_t ld;

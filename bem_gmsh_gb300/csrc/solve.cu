@@ -546,7 +546,7 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
   Timer ta(c, 0);
   ta.start(c->stream);
   // the FP64 comparison path keeps FP64 arithmetic throughout
-  const int prec = (mode == BEM_SOLVE_MIXED && kind == 0 && c->opt_far_df >= 1) ? 3 : 1;
+  const int prec = (mode == BEM_SOLVE_MIXED && c->opt_far_df >= 1) ? 3 : 1;
   rc = bem_assemble_system_dev(c, g, ph, BC, BV, npg, near_factor, mem, prec, A, ld, nullptr, b);
   ta.stop(c->stream);
   if (rc) return rc;

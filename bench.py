@@ -141,9 +141,9 @@ GEMM_TRAFFIC_CAPTURE = {"launch": "bulk update alone, trailing block 8064^2", "r
 
 
 def extra_configs(ctx):
-    """Config C4 (512 uneven star domains, batched solve) and C5 (adjoint
-    shape gradients of 64 domains x 1023 nodes), wall-clock through the
-    public API with host buffers."""
+    """Config C4 (512 uneven star domains, batched solve), C3 (plate with a
+    hole, 8196 DOF elasticity) and C5 (adjoint shape gradients of 64 domains
+    x 1023 nodes), wall-clock through the public API with host buffers."""
     import numpy as np
     from bem_gmsh_gb300.geometry import c4_node_counts, c4_domains, star_adjoint_case
     from bem_gmsh_gb300.api import solve_batch, adjoint_laplace, adjoint_laplace_batch, solve, tune_batch
@@ -173,6 +173,56 @@ def extra_configs(ctx):
                         "median_rel_err": float(np.median(errs))},
         "note": "wall clock through solve_batch with host buffers, after the autotuner's passes; "
                 "per-domain pipelines on the tuned number of worker streams"}
+    # C3: plate with a hole, 8196 DOF of 2-D elasticity, mixed vs FP64 GPU
+    from bem_gmsh_gb300.geometry import plate_with_hole
+    from bem_gmsh_gb300.api import recover_strain_stress, hoop_stress
+    s_inf = 1e8
+    plate = plate_with_hole(n_outer_el=1024, n_hole_el=342, p=2, sigma=s_inf)
+    for _ in range(2):
+        solve(plate, npg=16, mode="mixed", ctx=ctx)
+    tm, stm = [], []
+    for _ in range(10):
+        t0 = time.perf_counter()
+        _, stc = solve(plate, npg=16, mode="mixed", ctx=ctx, return_stats=True)
+        tm.append(time.perf_counter() - t0)
+        stm.append(stc)
+    x3 = plate.cache["x"].copy()
+    recover_strain_stress(plate, ctx=ctx)
+    hole = np.arange(plate.n - 3 * 342, plate.n)
+    Xh = np.asarray(plate.collocation[hole])
+    th = np.arctan2(Xh[:, 1], Xh[:, 0])
+    stt = hoop_stress(plate)[hole] / s_inf
+    top = np.abs(np.abs(th) - np.pi / 2) < 0.02
+    p64 = plate_with_hole(n_outer_el=1024, n_hole_el=342, p=2, sigma=s_inf)
+    solve(p64, npg=16, mode="fp64", ctx=ctx)
+    t64 = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        solve(p64, npg=16, mode="fp64", ctx=ctx)
+        t64.append(time.perf_counter() - t0)
+    x64 = p64.cache["x"]
+    free = np.asarray(plate.BC) == 1
+    nt3, n3 = plate.nt, plate.n
+    ent3 = float((2 * nt3) * (2 * nt3) + (2 * nt3) * (2 * n3))
+    asm_ms = statistics.mean(sv["t_assemble_ms"] for sv in stm)
+    out["plate_c3"] = {
+        "dof": 2 * nt3, "solves_per_s": 1.0 / statistics.mean(tm), "ms_per_solve": 1e3 * statistics.mean(tm),
+        "fp64_solves_per_s": 1.0 / statistics.mean(t64),
+        "speedup_mixed_vs_fp64": statistics.mean(t64) / statistics.mean(tm),
+        "rel_err_displacements_vs_fp64_gpu": float(np.linalg.norm(x3[free] - x64[free]) /
+                                                   np.linalg.norm(x64[free])),
+        "pinned_reactions_diff_over_load": float(np.max(np.abs(x3[~free] - x64[~free])) / s_inf),
+        "assembly_ms": asm_ms, "entries_per_s": ent3 / (asm_ms * 1e-3),
+        "factor_ms": statistics.mean(sv["t_factor_ms"] for sv in stm),
+        "refine_ms": statistics.mean(sv["t_refine_ms"] for sv in stm),
+        "gmres_iterations": int(max(sv["iterations"] for sv in stm)),
+        "kirsch_peak_hoop_stress": float(stt[top].mean()),
+        "note": "wall clock of api.solve with host buffers (10 mixed, 2 FP64 solves); mixed: Kelvin far "
+                "field in double-float, FP32/TF32 LU, FP64 GMRES; stage times are device time; H+G entries "
+                "(2nt)^2 + (2nt)(2n) per assembly; errors of the displacement unknowns (relative) and of the "
+                "three pinned reaction tractions (zero for this self-equilibrated load, relative to the "
+                "load); the hoop-stress peak at the top and bottom of the hole (3.879 in a converged oracle "
+                "mesh study); the full-size comparison with the FP64 oracle is tests/test_gpu_stress.py"}
     cases = [star_adjoint_case(341, p=2, seed=s) for s in range(64)]
     qts = []
     for d, tg in cases:

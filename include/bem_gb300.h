@@ -49,7 +49,7 @@ extern "C" {
 #define BEM_OPT_KERNEL_TIMING 2 /* 1: time kernel classes with CUDA events (bem_kernel_times) */
 #define BEM_OPT_FAR_DF 3        /* far-field Laplace entries of FP64 systems evaluated in double-float
                                    (FP32 pairs, ~1e-14 relative): 0 never, 1 (default) in mixed-precision
-                                   solves, 2 also in bem_assemble_system2d.  Kelvin stays FP64. */
+                                   solves, 2 also in bem_assemble_system2d.  Laplace and Kelvin. */
 #define BEM_OPT_GRAPHS 4        /* 1 (default): the mixed solve's factorization (equilibration, look-ahead
                                    LU, sweep couplings) is captured in a CUDA graph on the second call with
                                    unchanged buffers and replayed; 0: direct launches.  Not used while
