@@ -21,6 +21,9 @@ BEM_OPT_GRAPHS = 4
 BEM_OPT_PIVOT_FALLBACK = 5
 BEM_OPT_WAIT_LIMIT = 6
 BEM_OPT_INJECT = 7
+BEM_OPT_NEARFIELD = 8
+BEM_OPT_SINGULAR = 9
+NEARFIELD = {"tanp3c": 0, "plain": 1, "tangent": 5, "p3c": 6}
 BEM_NOALLOC_MAX_NT, BEM_NOALLOC_MAX_NE = 16384, 8192
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
                   "lu_panels", "lu_thin"]

@@ -69,14 +69,40 @@ def _ld(x) -> int:
     return x.shape[0]
 
 
+class _rules:
+    """The reference's per-problem quadrature knobs (`nearfield`,
+    src/Core/Integration.jl:41-93; `singular`, src/Core/Assembly_full.jl:
+    282-283) as context options for the duration of one call."""
+
+    def __init__(self, ctx, nearfield: str, singular: str):
+        if nearfield not in _lib.NEARFIELD:
+            raise ValueError(f"nearfield must be one of {sorted(_lib.NEARFIELD)}; got {nearfield!r}")
+        if singular not in ("guiggiani", "telles"):
+            raise ValueError(f"singular must be 'guiggiani' or 'telles'; got {singular!r}")
+        self.ctx, self.nf, self.sg = ctx, _lib.NEARFIELD[nearfield], int(singular == "telles")
+
+    def __enter__(self):
+        self.ctx.set_option(_lib.BEM_OPT_NEARFIELD, self.nf)
+        self.ctx.set_option(_lib.BEM_OPT_SINGULAR, self.sg)
+
+    def __exit__(self, *exc):
+        self.ctx.set_option(_lib.BEM_OPT_NEARFIELD, 0)
+        self.ctx.set_option(_lib.BEM_OPT_SINGULAR, 0)
+        return False
+
+
 def H_G_gpu(dad: BEMdata, T=np.float32, npg: int = 20, near: str = "cpu", near_factor: float = 1.5,
-            device: str = "cuda", out=None, ctx: _lib.Context | None = None, store: bool = True):
+            device: str = "cuda", out=None, ctx: _lib.Context | None = None, store: bool = True,
+            nearfield: str = "tanp3c", singular: str = "guiggiani"):
     """Dense H, G on the GPU (reference `H_G_gpu`).
 
     T: np.float32 (far field in FP32, near/singular FP64) or np.float64.
     near: "cpu" in the reference means near/singular entries by
     `integrate_element`; here they are computed on the GPU in FP64, so "cpu"
     and "gpu" are both accepted and give the full near correction.
+    nearfield ("tanp3c", "plain", "tangent", "p3c") and singular
+    ("guiggiani", "telles") select the near-singular map and the on-element
+    rule, as the reference's cached `nearfield` and `singular` do.
     device must be "cuda" (no CPU fallback).  `out=(H, G)` may pass
     preallocated column-major numpy arrays or CUDA tensors."""
     if device != "cuda":
@@ -100,14 +126,15 @@ def H_G_gpu(dad: BEMdata, T=np.float32, npg: int = 20, near: str = "cpu", near_f
     g, keep = geom_struct(dad, device=dev)
     mem = _lib.BEM_MEM_DEVICE if dev else _lib.BEM_MEM_HOST
     dt = _lib.BEM_F32 if T == np.float32 else _lib.BEM_F64
-    if isinstance(pr, Laplace):
-        rc = ctx.L.bem_assemble_laplace2d(ctx.h, g, float(pr.k), int(npg), float(near_factor), dt, mem,
-                                          _ptr(H), _ld(H), _ptr(G), _ld(G))
-    elif isinstance(pr, Elasticity):
-        rc = ctx.L.bem_assemble_kelvin2d(ctx.h, g, float(pr.mu), float(pr.nu_eff), int(npg),
-                                         float(near_factor), dt, mem, _ptr(H), _ld(H), _ptr(G), _ld(G))
-    else:
+    if not isinstance(pr, (Laplace, Elasticity)):
         raise ValueError(f"H_G_gpu supports Laplace and Elasticity; got {type(pr).__name__}")
+    with _rules(ctx, nearfield, singular):
+        if isinstance(pr, Laplace):
+            rc = ctx.L.bem_assemble_laplace2d(ctx.h, g, float(pr.k), int(npg), float(near_factor), dt, mem,
+                                              _ptr(H), _ld(H), _ptr(G), _ld(G))
+        else:
+            rc = ctx.L.bem_assemble_kelvin2d(ctx.h, g, float(pr.mu), float(pr.nu_eff), int(npg),
+                                             float(near_factor), dt, mem, _ptr(H), _ld(H), _ptr(G), _ld(G))
     ctx.check(rc, "H_G_gpu")
     if store:
         dad.set_cache(H=H, G=G)

@@ -97,7 +97,10 @@ __global__ void __launch_bounds__(64) singular_kernel(NearArgs a) {
   closest_point_1d(a.R, nodes, nn, pf, xa, dist);
   V2 nref{g.nx[e * nn], g.ny[e * nn]};
   double h[BEM_MAXNN * NC], gg[BEM_MAXNN * NC];
-  integrate_singular<NC>(a.R, a.ph, nodes, geo, pf, xa, nref, h, gg);
+  if (a.R.singular == 1)
+    integrate_singular_telles<NC>(a.R, a.ph, nodes, geo, pf, xa, nref, h, gg);
+  else
+    integrate_singular<NC>(a.R, a.ph, nodes, geo, pf, xa, nref, h, gg);
   for (int ar = 0; ar < DOF; ++ar) {
     const size_t row = (size_t)DOF * i + ar;
     double rs[DOF], bs = 0.0;

@@ -35,6 +35,8 @@ int ensure_workers(bem_ctx* c, int w) {
     s->opt_pivot_fallback = c->opt_pivot_fallback;
     s->opt_wait_limit = c->opt_wait_limit;
     s->opt_inject = c->opt_inject;
+    s->opt_nearfield = c->opt_nearfield;
+    s->opt_singular = c->opt_singular;
   }
   return BEM_OK;
 }

@@ -308,6 +308,8 @@ int bem_stage_geom(bem_ctx* c, const bem_geom2d* g, int npg, int mem, GeomDev& g
     std::memcpy(ew, h, sizeof(double) * nn);
   }
   build_rules(g, npg, ew, R);
+  R.nearfield = (unsigned char)c->opt_nearfield;
+  R.singular = (unsigned char)c->opt_singular;
   gd.nt = g->nt;
   gd.n = g->n;
   gd.ne = g->ne;

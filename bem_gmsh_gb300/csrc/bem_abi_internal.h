@@ -36,6 +36,8 @@ struct bem_ctx {
   int opt_pivot_fallback = 1;      // BEM_OPT_PIVOT_FALLBACK
   int opt_wait_limit = 1 << 20;    // BEM_OPT_WAIT_LIMIT
   int opt_inject = 0;              // BEM_OPT_INJECT
+  int opt_nearfield = 0;           // BEM_OPT_NEARFIELD
+  int opt_singular = 0;            // BEM_OPT_SINGULAR
   // why the last mixed solve did not converge (MIXED_*)
   enum { MIXED_OK = 0, MIXED_PIVOT = 1, MIXED_STAGNATION = 2, MIXED_CAP = 3 };
   int mixed_fail = MIXED_OK;

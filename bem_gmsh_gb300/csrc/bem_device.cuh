@@ -32,7 +32,10 @@ struct Rules {
   int nn;    // field nodes per element (p+1)
   int ngeo;  // CAD nodes per element, 0 = geometry from the field nodes
   int npg;   // near-field Gauss rule size
-  int pad_;
+  // near-field map (`nearfield`, Integration.jl:41-93): 0 tanp3c, 1 plain
+  // Gauss, 5 tangent, 6 p3c; on-element rule (`singular`,
+  // Assembly_full.jl:282-283): 0 interpolated Guiggiani, 1 Telles
+  unsigned char nearfield, singular, pad0_, pad1_;
   double leg_x[BEM_MAXNN], leg_bw[BEM_MAXNN], leg_D[BEM_MAXNN * BEM_MAXNN];
   double geo_x[BEM_MAXGEO], geo_bw[BEM_MAXGEO], geo_D[BEM_MAXGEO * BEM_MAXGEO];
   double qsi[BEM_MAXNPG], w[BEM_MAXNPG];
@@ -351,9 +354,17 @@ __device__ inline void integrate_near(const Rules& R, const Physics& ph, const V
                                V2 pf, V2 nref, double* h, double* g) {
   const int nn = R.nn;
   double eta[BEM_MAXMAP], ww[BEM_MAXMAP];
-  double z0, e0;
-  complex_pole_1d(R, nodes, nn, pf, z0, e0);
-  int m = tanp3ctrans(R, z0, e0, eta, ww);
+  int m;
+  if (R.nearfield == 1) {  // plain Gauss rule
+    m = R.npg;
+    for (int i = 0; i < m; ++i) { eta[i] = R.qsi[i]; ww[i] = R.w[i]; }
+  } else {
+    double z0, e0;
+    complex_pole_1d(R, nodes, nn, pf, z0, e0);
+    if (R.nearfield == 5) m = nm::tangenttrans(R, nm::ieee(z0), nm::ieee(e0), eta, ww);
+    else if (R.nearfield == 6) m = nm::p3ctrans(R, nm::ieee(z0), nm::ieee(e0), eta, ww);
+    else m = tanp3ctrans(R, z0, e0, eta, ww);
+  }
   for (int c = 0; c < nn * NC; ++c) h[c] = g[c] = 0.0;
   double flip = 1.0;
   for (int i = 0; i < m; ++i) {
@@ -376,6 +387,54 @@ __device__ inline void integrate_near(const Rules& R, const Physics& ph, const V
       for (int c = 0; c < NC; ++c) {
         h[j * NC + c] += T[c] * Nj;
         g[j * NC + c] += U[c] * Nj;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Telles on-element rule (_telles_map, _integrate_singular_telles!,
+// Assembly_full.jl:467-528): the near-field Gauss rule through the cubic map
+// whose derivative vanishes at the source's parent coordinate a.  The map's
+// constants use the correctly rounded cbrt and explicit IEEE operations, so
+// they are the bits of a CPU restatement.
+// --------------------------------------------------------------------------
+template <int NC>
+__device__ inline void integrate_singular_telles(const Rules& R, const Physics& ph, const V2* nodes,
+                                                 const V2* geo, V2 pf, double a, V2 nref, double* h, double* g) {
+  using nm::ieee;
+  const int nn = R.nn;
+  for (int c = 0; c < nn * NC; ++c) h[c] = g[c] = 0.0;
+  a = fmin(fmax(a, -0.9999999999999999), 0.9999999999999999);
+  const ieee eet = a;
+  const ieee eest = eet * eet - ieee(1.0);
+  const ieee term1 = crm::cr_cbrt((eet * eest + abs(eest)).v);
+  const ieee term2 = crm::cr_cbrt((eet * eest - abs(eest)).v);
+  const ieee Gm = term1 + term2 + eet;
+  const ieee Q = ieee(1.0) + ieee(3.0) * (Gm * Gm);
+  const ieee A = ieee(1.0) / Q, B = ieee(-3.0) * Gm / Q, Cc = ieee(3.0) * (Gm * Gm) / Q, D = -B;
+  for (int i = 0; i < R.npg; ++i) {
+    const ieee gm = R.qsi[i];
+    const double eta = (A * (gm * gm * gm) + B * (gm * gm) + Cc * gm + D).v;
+    const double Jt = (ieee(3.0) * A * (gm * gm) + ieee(2.0) * B * gm + Cc).v;
+    double N[BEM_MAXNN];
+    V2 pg, dx;
+    shape_geom(R, nodes, geo, eta, N, pg, dx);
+    const double J = vnorm(dx.x, dx.y);
+    if (J < 1e-30) continue;
+    const double rx = pg.x - pf.x, ry = pg.y - pf.y;
+    if (vnorm(rx, ry) < 1e-30) continue;
+    const double invJ = 1.0 / J;
+    double nxq = dx.y * invJ, nyq = -(dx.x * invJ);
+    if (nxq * nref.x + nyq * nref.y < 0) { nxq = -nxq; nyq = -nyq; }
+    double U[4], T[4];
+    eval_kernel<NC>(ph, rx, ry, nxq, nyq, U, T);
+    const double wJ = Jt * R.w[i] * J;
+    for (int j = 0; j < nn; ++j) {
+      const double Nj = N[j] * wJ;
+      for (int c = 0; c < NC; ++c) {
+        g[j * NC + c] += U[c] * Nj;
+        h[j * NC + c] += T[c] * Nj;
       }
     }
   }

@@ -36,7 +36,10 @@ __global__ void __launch_bounds__(IT) interior_laplace_kernel(GeomDev g, Rules R
     closest_point_1d(R, nodes, nn, pf, xa, dist);
     const V2 nref{g.nx[e * nn], g.ny[e * nn]};
     if (dist <= 1e-12)
-      integrate_singular<1>(R, ph, nodes, geo, pf, xa, nref, h, gg);
+      if (R.singular == 1)
+        integrate_singular_telles<1>(R, ph, nodes, geo, pf, xa, nref, h, gg);
+      else
+        integrate_singular<1>(R, ph, nodes, geo, pf, xa, nref, h, gg);
     else
       integrate_near<1>(R, ph, nodes, geo, pf, nref, h, gg);
     for (int a = 0; a < nn; ++a) {

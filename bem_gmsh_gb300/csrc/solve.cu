@@ -597,6 +597,16 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
     c->opt_wait_limit = value;
     return BEM_OK;
   }
+  if (option == BEM_OPT_NEARFIELD) {
+    if (value != 0 && value != 1 && value != 5 && value != 6) return BEM_ERR_UNSUPPORTED;
+    c->opt_nearfield = value;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_SINGULAR) {
+    if (value != 0 && value != 1) return BEM_ERR_INVALID;
+    c->opt_singular = value;
+    return BEM_OK;
+  }
   if (option == BEM_OPT_INJECT) {
     if (value < 0 || value > 3) return BEM_ERR_INVALID;
     c->opt_inject = value;

@@ -69,6 +69,13 @@ extern "C" {
                                    triangular sweeps publish their results under another epoch than
                                    the one their readers wait for, so those bounded waits run out
                                    (BEM_ERR_INTERNAL, the context stays usable) */
+#define BEM_OPT_NEARFIELD 8     /* near-singular map of the element integrals, the reference's `nearfield`
+                                   knob (src/Core/Integration.jl:41-93, set per problem with set_cache!):
+                                   0 (default) tanp3c, 1 plain Gauss rule, 5 tangent (eq. 41), 6 complete
+                                   cubic p3c; the sinh-family maps return BEM_ERR_UNSUPPORTED */
+#define BEM_OPT_SINGULAR 9      /* on-element rule, the reference's `singular` knob
+                                   (src/Core/Assembly_full.jl:282-283): 0 (default) interpolated
+                                   Guiggiani, 1 Telles cubic map of the npg Gauss rule */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */

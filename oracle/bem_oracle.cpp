@@ -1078,8 +1078,8 @@ void integrate_singular_telles(const Ctx& C, const V2* nodes, const V2* geo, V2 
   a = std::min(std::max(a, std::nextafter(-1.0, 0.0)), std::nextafter(1.0, 0.0));
   double eet = a;
   double eest = eet * eet - 1;
-  double term1 = std::cbrt(eet * eest + std::fabs(eest));
-  double term2 = std::cbrt(eet * eest - std::fabs(eest));
+  double term1 = cr_cbrt(eet * eest + std::fabs(eest));
+  double term2 = cr_cbrt(eet * eest - std::fabs(eest));
   double Gm = term1 + term2 + eet;
   double Q = 1 + 3 * (Gm * Gm);
   double A = 1 / Q, B = -3 * Gm / Q, Cc = 3 * (Gm * Gm) / Q, D = -B;

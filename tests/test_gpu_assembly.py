@@ -237,3 +237,31 @@ def test_full_size_parity_every_entry(orc):
     print(f"H: rel {eh:.2e} max entry {dh:.2e}; G: rel {eg:.2e} max entry {dg:.2e}; "
           f"near entries max rel: G {gn.max():.2e}, H {hn.max():.2e}")
     assert gn.max() < 1e-10
+
+
+@pytest.mark.parametrize("nearfield", ["plain", "tangent", "p3c"])
+def test_nearfield_maps_match_oracle(orc, nearfield):
+    """The reference's `nearfield` knob (src/Core/Integration.jl:41-93): the
+    plain Gauss rule and the tangent and complete-cubic maps, Laplace and
+    Kelvin, against the oracle with the same map (FP64, every entry)."""
+    for dad in (star_domain(150, p=2, seed=12, pontointerno=True),
+                quadrado_elasticity(ndiv=9, ordem=2, props=Elasticity(1.0, 0.3, 1.0), pontointerno=True)):
+        Hr, Gr = orc.assemble(dad, npg=16, nearfield=nearfield, store=False)
+        H, G = H_G_gpu(dad, T=np.float64, npg=16, nearfield=nearfield, store=False)
+        check64(H, Hr, f"H {nearfield}")
+        check64(G, Gr, f"G {nearfield}")
+
+
+def test_telles_on_element_rule_matches_oracle(orc):
+    """`singular=:telles` (src/Core/Assembly_full.jl:282-283, 467-528), which the
+    reference's Kelvin H_G_gpu accepts (src/Elasticity/Assembly_GPU.jl:23):
+    Kelvin and Laplace on curved quadratic elements against the oracle's
+    Telles rule, and close to the interpolated Guiggiani result."""
+    pr = Elasticity(E=210e9, nu=0.3, plane_strain=True)
+    for dad in (star_domain(80, p=2, seed=5, props=pr), star_domain(120, p=2, seed=6, pontointerno=True)):
+        Hr, Gr = orc.assemble(dad, npg=16, singular="telles", store=False)
+        H, G = H_G_gpu(dad, T=np.float64, npg=16, singular="telles", store=False)
+        check64(H, Hr, "H telles")
+        check64(G, Gr, "G telles")
+        Hg, Gg = H_G_gpu(dad, T=np.float64, npg=16, store=False)
+        assert rel(G, Gg) < 1e-3  # two quadratures of the same log-singular integrals
