@@ -3,4 +3,4 @@ from .geometry import (BEMdata, Laplace, Elasticity, quadrado, quadrado_elastici
                        plate_with_hole, ana_laplace_linear, ana_laplace_expcos,
                        ana_elasticity_patch, attach_analytical, apply_analytical_bc, rel_error,
                        rel_error_flux, from_cad, from_nodes, star_adjoint_case, internal_grid,
-                       point_in_domain)
+                       point_in_domain, format2d)

@@ -578,6 +578,37 @@ def discretize(cad, p: int, ctx: _lib.Context | None = None):
     return nodes, normal, J.reshape(ne, p + 1), L, wi
 
 
+def cells_array(cells) -> np.ndarray:
+    """Corner arrays of triangles and quadrangles as (ncell, 4, 2), a triangle
+    repeating its last corner (the layout of bem_orient2d)."""
+    out = np.empty((len(cells), 4, 2))
+    for i, c in enumerate(cells):
+        c = np.asarray(c, dtype=np.float64)
+        out[i, :len(c)] = c
+        out[i, len(c):] = c[-1]
+    return out
+
+
+def orient_normals(dad: BEMdata, cells, ctx: _lib.Context | None = None) -> np.ndarray:
+    """Flip, in place, the normals of every element whose point 0.1 L behind
+    its first node lies in none of the domain `cells` (`_orient_normals_outward!`,
+    src/Core/Input.jl:376-389), on the device; returns the flipped mask (ne,)."""
+    ctx = ctx or _lib.default_context()
+    n, p = dad.n, dad.p
+    px = np.ascontiguousarray(dad.collocation[:n, 0])
+    py = np.ascontiguousarray(dad.collocation[:n, 1])
+    nx = np.ascontiguousarray(dad.normal[:, 0])
+    ny = np.ascontiguousarray(dad.normal[:, 1])
+    elen = np.ascontiguousarray(dad.elem_length, dtype=np.float64)
+    cz = np.ascontiguousarray(cells_array(cells)) if len(cells) else np.zeros((1, 4, 2))
+    flipped = np.zeros(dad.ne, np.int32)
+    rc = ctx.L.bem_orient2d(ctx.h, dad.ne, p, _ptr(px), _ptr(py), _ptr(nx), _ptr(ny), _ptr(elen), len(cells),
+                            _ptr(cz), _lib.BEM_MEM_HOST, _ptr(flipped))
+    ctx.check(rc, "orient_normals")
+    dad.normal = np.ascontiguousarray(np.stack([nx, ny], axis=-1))
+    return flipped.astype(bool)
+
+
 def dibem_fd(dad: BEMdata, rbf: str = "PHS3", dtype=np.float64, epsa: float = 1e-16,
              ctx: _lib.Context | None = None):
     """Dense pairwise DIBEM matrices over all collocation points

@@ -20,6 +20,7 @@ All host-side numpy: this is input preparation, not the hot path.
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 from typing import Callable, Optional
 
@@ -221,6 +222,54 @@ def from_cad(name, cad, p, properties, bc_type, bc_value, internal=None, region=
         properties=properties, BC=bt.reshape(-1).astype(np.int32),
         BV=bv.reshape(-1), region=np.asarray(region if region is not None else np.zeros(ne), np.int64))
     return dad.contiguous()
+
+
+def format2d(path: str, properties, tipo: Optional[int] = None, pontointerno: bool = True,
+             discretize=None, orient=None) -> BEMdata:
+    """`format2d(file, properties; tipo, pontointerno)` (src/Core/Input.jl:108-197)
+    from a Gmsh ASCII mesh file: the boundary's line elements (their nodes as
+    equispaced CAD nodes of degree p = the mesh order; p + 1 Gauss-Legendre
+    collocation nodes each), boundary conditions from each curve's physical
+    name ("type;value" pairs, `parse_pairs`), normals oriented outward with
+    the 2-D cells (`_orient_normals_outward!`) and, with pontointerno, the
+    cells' centroids as internal points.  The discretisation and the
+    orientation run on the device (`api.discretize`, `api.orient_normals`);
+    `discretize(cad, p)` and `orient(dad, cells)` replace them."""
+    from .msh import read_msh, parse_pairs
+    from . import api
+    m = read_msh(path)
+    p = m.order
+    if tipo is not None and int(tipo) != p:
+        raise ValueError(f"format2d: the mesh has order {p}; changing it (tipo={tipo}) needs Gmsh")
+    ndof = properties.ndof
+    ne = m.lines.shape[0]
+    bt = np.ones((ne, ndof), np.int32)
+    bv = np.zeros((ne, ndof))
+    for e in range(ne):
+        nm = m.names.get(int(m.line_entity[e]))
+        if nm is None:
+            continue
+        ints, floats = parse_pairs(nm)
+        k = min(len(ints), ndof)
+        bt[e, :k] = ints[:k]
+        bv[e, :k] = floats[:k]
+    cells = [c for c in m.cells if abs(polygon_area(c)) >= 1e-18]
+    internal = np.array([c.mean(axis=0) for c in cells]) if (pontointerno and cells) else None
+    dad = from_cad(os.path.basename(path), m.lines, p, properties, bt, bv, internal=None,
+                   region=m.line_entity, discretize=discretize or api.discretize)
+    (orient or api.orient_normals)(dad, cells)
+    if internal is not None:
+        dad.collocation = np.ascontiguousarray(np.vstack([dad.collocation, internal]))
+    dad.cache["cells"] = cells
+    return dad.contiguous()
+
+
+def polygon_area(verts) -> float:
+    """Signed area of a closed polygon, counter-clockwise positive
+    (`polygon_area`, src/Core/Input.jl:287-298)."""
+    v = np.asarray(verts, dtype=np.float64)
+    x, y = v[:, 0], v[:, 1]
+    return 0.5 * float(np.sum(x * np.roll(y, -1) - np.roll(x, -1) * y))
 
 
 def from_nodes(name, X, p, properties, bc_type, bc_value) -> BEMdata:

@@ -303,6 +303,20 @@ int bem_discretize2d(bem_ctx* ctx, int ne, int ngeo, int p, const double* cad_x,
                      double* elem_weight);
 
 /*
+ * Outward normals of a 2-D boundary mesh -- replaces `_orient_normals_outward!`
+ * (src/Core/Input.jl:376-389) of `format2d`: for element e (nodes e(p+1) ..
+ * e(p+1)+p of px, py, nx, ny; length elen[e]) the point 0.1 elen[e] behind
+ * its first node along -n must lie inside one of the ncell domain cells (the
+ * 2-D elements of the mesh, even-odd test of `point_in_polygon`, :331-345),
+ * else all of the element's normals are negated in place; flipped[e] = 1
+ * then.  cells: ncell x 4 corners (x, y), a triangle repeating its last
+ * corner.  ncell = 0 leaves the normals unchanged, as the reference does
+ * without a 2-D mesh.  mem says where all arrays live.
+ */
+int bem_orient2d(bem_ctx* ctx, int ne, int p, const double* px, const double* py, double* nx, double* ny,
+                 const double* elen, int ncell, const double* cells, int mem, int32_t* flipped);
+
+/*
  * Shape gradient by the adjoint method (no reference counterpart; built on
  * the path's assembly and solve, src/Core/Assembly_full.jl:61-175 and
  * src/Core/Boundary_conditions.jl:20-75).  Laplace, elements with their

@@ -311,3 +311,42 @@ def timed_pipeline(dad, npg=16, threads=0):
     t3 = time.perf_counter()
     split_sol(dad, x)
     return dict(assemble=t1 - t0, apply_bc=t2 - t1, lu=t3 - t2, total=t3 - t0, x=x)
+
+
+def point_in_polygon(p, verts):
+    """Even-odd ray test, boundary outside (`point_in_polygon`,
+    src/Core/Input.jl:331-345)."""
+    inside = False
+    nv = len(verts)
+    j = nv - 1
+    for i in range(nv):
+        yi, yj = verts[i][1], verts[j][1]
+        if (yi > p[1]) != (yj > p[1]):
+            xint = (verts[j][0] - verts[i][0]) * (p[1] - yi) / (yj - yi + 1e-30) + verts[i][0]
+            if p[0] < xint:
+                inside = not inside
+        j = i
+    return inside
+
+
+def orient_normals(nodes, normal, elen, p, cells):
+    """`_orient_normals_outward!` (src/Core/Input.jl:376-389): the normals of
+    element e flip unless the point 0.1 L behind its first node lies in a
+    cell.  nodes, normal: (n, 2); returns (oriented normals, flipped mask)."""
+    normal = np.array(normal, dtype=np.float64)
+    nn = p + 1
+    ne = len(elen)
+    flipped = np.zeros(ne, bool)
+    if not len(cells):
+        return normal, flipped
+    for e in range(ne):
+        i0 = e * nn
+        d = 0.1 * float(elen[e])
+        if d < 1e-16:
+            continue
+        pt = (nodes[i0][0] - d * normal[i0][0], nodes[i0][1] - d * normal[i0][1])
+        if any(point_in_polygon(pt, c) for c in cells):
+            continue
+        normal[i0:i0 + nn] = -normal[i0:i0 + nn]
+        flipped[e] = True
+    return normal, flipped
