@@ -31,7 +31,7 @@ def test_device_orientation_matches_oracle(orc, p):
     nodes, normal, J, L, w = discretize_curves(m.lines, p)
     ref, flipped = orc.orient_normals(nodes.reshape(-1, 2), normal.reshape(-1, 2), L, p, m.cells)
     assert flipped.sum() == 2 * 8  # the two clockwise sides
-    assert np.max(np.abs(dad.normal - ref)) < 1e-14
+    assert np.max(np.abs(dad.normal - ref)) < 1e-13  # device vs host discretisation rounding
     assert np.max(np.abs(dad.collocation - nodes.reshape(-1, 2))) < 1e-15
 
 
