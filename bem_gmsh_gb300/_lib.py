@@ -102,6 +102,8 @@ def load(build_if_missing: bool = False):
                               VP, VP], ctypes.c_int),
         "bem_discretize2d": ([ctx_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, VP, VP, ctypes.c_int, VP, VP,
                               VP, VP, VP, VP, VP], ctypes.c_int),
+        "bem_dibem_ifid_near2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, ctypes.c_int, D, D, ctypes.c_int,
+                                   ctypes.c_int, VP, VP], ctypes.c_int),
         "bem_orient2d": ([ctx_p, ctypes.c_int, ctypes.c_int, VP, VP, VP, VP, VP, ctypes.c_int, VP, ctypes.c_int,
                           VP], ctypes.c_int),
         "bem_dibem_fd2d": ([ctx_p, ctypes.c_int, VP, VP, ctypes.c_int, D, D, ctypes.c_int, D, ctypes.c_int,

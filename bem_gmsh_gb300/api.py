@@ -539,10 +539,12 @@ RBF_KINDS = {"PHS1": 1, "PHS2": 2, "PHS3": 3, "PHS4": 4, "PHS5": 5, "PHS6": 6, "
 
 
 def dibem_ifid(dad: BEMdata, rbf: str = "PHS3", dtype=np.float64, epsa: float = 1e-16, near_factor: float = 1.5,
-               ctx: _lib.Context | None = None):
-    """Far boundary sums IF, ID of the DIBEM domain integrals at every
-    collocation point (`_dibem_IFID_ka`, src/Laplace/DIBEM_GPU.jl:209-270);
-    near pairs are skipped for the caller's quadrature correction."""
+               ctx: _lib.Context | None = None, near: bool = False, npg: int = 16):
+    """Boundary sums IF, ID of the DIBEM domain integrals at every collocation
+    point: the far sums (`_dibem_IFID_ka`, src/Laplace/DIBEM_GPU.jl:209-270),
+    which skip near and on-element pairs, and with `near` also their npg-point
+    Gauss-rule correction (`_dibem_correct_near_cpu!`, :272-300, FP64), which
+    together are the reference's IF, ID."""
     ctx = ctx or _lib.default_context()
     if not isinstance(dad.properties, Laplace):
         raise ValueError("dibem_ifid supports Laplace meshes")
@@ -553,6 +555,12 @@ def dibem_ifid(dad: BEMdata, rbf: str = "PHS3", dtype=np.float64, epsa: float = 
     rc = ctx.L.bem_dibem_ifid2d(ctx.h, g, float(dad.properties.k), RBF_KINDS[rbf], float(epsa), float(near_factor),
                                 dt, _lib.BEM_MEM_HOST, _ptr(IF), _ptr(ID))
     ctx.check(rc, "dibem_ifid")
+    if near:
+        IF = np.ascontiguousarray(IF, dtype=np.float64)
+        ID = np.ascontiguousarray(ID, dtype=np.float64)
+        rc = ctx.L.bem_dibem_ifid_near2d(ctx.h, g, float(dad.properties.k), RBF_KINDS[rbf], float(epsa),
+                                         float(near_factor), int(npg), _lib.BEM_MEM_HOST, _ptr(IF), _ptr(ID))
+        ctx.check(rc, "dibem_ifid_near")
     return IF, ID
 
 

@@ -253,6 +253,85 @@ __global__ void __launch_bounds__(128) dibem_ifid_kernel(GeomDev g, IfidRule rw,
   atomicAdd(ID + i, aD);
 }
 
+// Near-pair correction of IF and ID (`_dibem_correct_near_cpu!`,
+// src/Laplace/DIBEM_GPU.jl:272-300): for every element near point i (the
+// assembly's exact test) or holding it, the npg-point Gauss rule on the
+// element's field interpolant (`_rim_build_elements`,
+// src/Core/DIBEM_common.jl:112-171: rule points y_q, normals tan2normal of
+// the tangent aligned with the element's first nodal normal, w_q J_q),
+//   IF_i += phi_int(R) w_q J_q (r . n_q) / R^2,  ID_i += rad(R) w_q J_q (r . n_q) / R^2
+// with r = y_q - x_i, points closer than 1e-14 skipped.  FP64.  The block's
+// 16 elements and their rule points are built once in shared memory; each
+// thread takes one point.
+constexpr int NR_EC = 16;
+__global__ void __launch_bounds__(128) dibem_near_kernel(GeomDev g, Rules R, int rbf, double kcond, double epsa,
+                                                         double nf, double* __restrict__ IF,
+                                                         double* __restrict__ ID) {
+  __shared__ double sx[NR_EC * BEM_MAXNN], sy[NR_EC * BEM_MAXNN];
+  __shared__ double qy[NR_EC * BEM_MAXNPG][5];  // y.x, y.y, n.x, n.y, w J
+  __shared__ double belen[NR_EC];
+  const int nn = g.nn, npg = R.npg;
+  const int e0 = blockIdx.y * NR_EC;
+  const int nel = min(NR_EC, g.ne - e0);
+  for (int idx = threadIdx.x; idx < nel * nn; idx += blockDim.x) {
+    sx[idx] = g.px[e0 * nn + idx];
+    sy[idx] = g.py[e0 * nn + idx];
+  }
+  for (int el = threadIdx.x; el < nel; el += blockDim.x) belen[el] = g.elen[e0 + el];
+  __syncthreads();
+  for (int t = threadIdx.x; t < nel * npg; t += blockDim.x) {
+    const int el = t / npg, q = t - el * npg;
+    double L[BEM_MAXNN], dL[BEM_MAXNN];
+    shapefun(R.leg_x, R.leg_bw, R.leg_D, nn, R.qsi[q], L, dL);
+    double px = 0, py = 0, dx = 0, dy = 0;
+    for (int k = 0; k < nn; ++k) {
+      px += L[k] * sx[el * nn + k];
+      py += L[k] * sy[el * nn + k];
+      dx += dL[k] * sx[el * nn + k];
+      dy += dL[k] * sy[el * nn + k];
+    }
+    const double J = sqrt(dx * dx + dy * dy);
+    const int j0 = (e0 + el) * nn;
+    const double rx = g.nx[j0], ry = g.ny[j0];
+    double ux = rx, uy = ry;
+    if (!(J < 1e-16)) { ux = dy / J; uy = -dx / J; }
+    if (ux * rx + uy * ry < 0) { ux = -ux; uy = -uy; }
+    qy[t][0] = px;
+    qy[t][1] = py;
+    qy[t][2] = ux;
+    qy[t][3] = uy;
+    qy[t][4] = J < 1e-16 ? 0.0 : R.w[q] * J;
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.nt) return;
+  const V2 pf{g.px[i], g.py[i]};
+  const double radc = 1.0 / (8.0 * kPi * kcond);
+  double aF = 0.0, aD = 0.0;
+  for (int el = 0; el < nel; ++el) {
+    const int e = e0 + el;
+    const bool on = i >= e * nn && i < (e + 1) * nn;
+    if (!on) {
+      V2 xg[BEM_MAXNN];
+      for (int k = 0; k < nn; ++k) xg[k] = V2{sx[el * nn + k], sy[el * nn + k]};
+      if (!near_element(pf, xg, nn, belen[el], nf)) continue;
+    }
+    for (int q = 0; q < npg; ++q) {
+      const double* Y = qy[el * npg + q];
+      if (Y[4] == 0.0) continue;
+      const double rx = Y[0] - pf.x, ry = Y[1] - pf.y;
+      const double R2 = rx * rx + ry * ry;
+      const double Rr = sqrt(R2);
+      if (Rr < 1e-14) continue;
+      const double wJn = Y[4] * ((Y[2] * rx + Y[3] * ry) / R2);
+      aF += dibem_phi_int<double>(rbf, Rr, kcond, epsa) * wJn;
+      aD += -(2.0 * R2 * log(Rr) - R2) * radc * wJn;
+    }
+  }
+  if (aF != 0.0) atomicAdd(IF + i, aF);
+  if (aD != 0.0) atomicAdd(ID + i, aD);
+}
+
 }  // namespace
 }  // namespace bem
 
@@ -365,5 +444,43 @@ extern "C" int bem_dibem_fd2d(bem_ctx* c, int nt, const double* px, const double
   }
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return c->cuda_fail(e, "dibem");
+  return BEM_OK;
+}
+
+extern "C" int bem_dibem_ifid_near2d(bem_ctx* c, const bem_geom2d* geom, double k, int rbf, double epsa,
+                                     double near_factor, int npg, int mem, double* IF, double* ID) {
+  if (!c || !geom || !IF || !ID) return BEM_ERR_INVALID;
+  if (!((rbf >= 1 && rbf <= 7) || rbf == 10)) return BEM_ERR_INVALID;
+  if (mem != BEM_MEM_HOST && mem != BEM_MEM_DEVICE) return BEM_ERR_INVALID;
+  if (!(k > 0) || !(near_factor >= 0)) return BEM_ERR_INVALID;
+  int rc = bem_check_geom(geom, npg, near_factor);
+  if (rc) return rc;
+  CallScope cs(c);
+  cudaSetDevice(c->device);
+  GeomDev gd;
+  Rules R;
+  rc = bem_stage_geom(c, geom, npg, mem, gd, R);
+  if (rc) return rc;
+  const size_t nt = (size_t)gd.nt;
+  double *dF = IF, *dD = ID;
+  if (mem == BEM_MEM_HOST) {
+    double* o = (double*)c->get(bem_ctx::SLOT_OUT2, 2 * sizeof(double) * nt);
+    if (!o) return BEM_ERR_NOMEM;
+    dF = o;
+    dD = o + nt;
+    cudaMemcpyAsync(dF, IF, sizeof(double) * nt, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dD, ID, sizeof(double) * nt, cudaMemcpyHostToDevice, c->stream);
+  }
+  dim3 grid((unsigned)((nt + 127) / 128), (unsigned)((gd.ne + NR_EC - 1) / NR_EC));
+  dibem_near_kernel<<<grid, 128, 0, c->stream>>>(gd, R, rbf, k, epsa, near_factor, dF, dD);
+  count_launches(1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem_near_kernel");
+  if (mem == BEM_MEM_HOST) {
+    cudaMemcpyAsync(IF, dF, sizeof(double) * nt, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(ID, dD, sizeof(double) * nt, cudaMemcpyDeviceToHost, c->stream);
+  }
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "dibem_ifid_near");
   return BEM_OK;
 }

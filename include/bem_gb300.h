@@ -303,6 +303,20 @@ int bem_discretize2d(bem_ctx* ctx, int ne, int ngeo, int p, const double* cad_x,
                      double* elem_weight);
 
 /*
+ * Near-pair correction of the DIBEM boundary sums -- replaces
+ * `_dibem_correct_near_cpu!` (src/Laplace/DIBEM_GPU.jl:272-300), which the
+ * reference runs on the host after `_dibem_IFID_ka`: adds to IF, ID (FP64,
+ * [nt], in and out) the npg-point Gauss-rule integrals of every element near
+ * a point (the assembly's near test, near_factor) or holding it, on the
+ * element's field interpolant (`_rim_build_elements`,
+ * src/Core/DIBEM_common.jl:112-171).  With bem_dibem_ifid2d (whose far sums
+ * skip exactly those pairs) it gives the reference's IF, ID.  rbf as in
+ * bem_dibem_fd2d; mem says where IF, ID live (geometry as in the other calls).
+ */
+int bem_dibem_ifid_near2d(bem_ctx* ctx, const bem_geom2d* geom, double k, int rbf, double epsa,
+                          double near_factor, int npg, int mem, double* IF, double* ID);
+
+/*
  * Outward normals of a 2-D boundary mesh -- replaces `_orient_normals_outward!`
  * (src/Core/Input.jl:376-389) of `format2d`: for element e (nodes e(p+1) ..
  * e(p+1)+p of px, py, nx, ny; length elen[e]) the point 0.1 elen[e] behind

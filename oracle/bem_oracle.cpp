@@ -1617,6 +1617,68 @@ int orc_dibem_ifid2d(const OrcGeom* og, double k, int rbf, double epsa, double n
   return 0;
 }
 
+// Near-pair correction of the DIBEM boundary sums, restating
+// `_dibem_correct_near_cpu!` (src/Laplace/DIBEM_GPU.jl:272-300) with the
+// element rules of `_rim_build_elements` (src/Core/DIBEM_common.jl:112-171):
+// for every element e near point i (the assembly's near test) or holding it,
+// the npg-point Gauss rule on the element's field interpolant,
+//   IF_i += phi_int(R) w_q J_q (r . n_q) / R^2,  ID_i += rad(R) w_q J_q (r . n_q) / R^2
+// (r = y_q - x_i, points with R < 1e-14 skipped, n_q aligned with the
+// element's first nodal normal).  Adds to IF, ID.
+int orc_dibem_ifid_near2d(const OrcGeom* og, double k, int rbf, double epsa, double near_factor, int npg,
+                          double* IF, double* ID) {
+  Geom g = to_geom(og);
+  const int nn = g.p + 1;
+  Poly leg = make_legendre(g.p);
+  std::vector<double> qsi, w;
+  gauss_legendre(npg, qsi, w);
+  std::vector<double> yx(g.ne * npg), yy(g.ne * npg), nxq(g.ne * npg), nyq(g.ne * npg), wJ(g.ne * npg);
+  for (int e = 0; e < g.ne; ++e) {
+    const V2 nref{g.nx[e * nn], g.ny[e * nn]};
+    for (int q = 0; q < npg; ++q) {
+      double L[16], dL[16];
+      shapefun(leg, qsi[q], L, dL);
+      double px = 0, py = 0, dx = 0, dy = 0;
+      for (int k2 = 0; k2 < nn; ++k2) {
+        px += L[k2] * g.px[e * nn + k2];
+        py += L[k2] * g.py[e * nn + k2];
+        dx += dL[k2] * g.px[e * nn + k2];
+        dy += dL[k2] * g.py[e * nn + k2];
+      }
+      const double J = std::sqrt(dx * dx + dy * dy);
+      double ux = nref.x, uy = nref.y;
+      if (!(J < 1e-16)) { ux = dy / J; uy = -dx / J; }
+      if (ux * nref.x + uy * nref.y < 0) { ux = -ux; uy = -uy; }
+      const int t = e * npg + q;
+      yx[t] = px; yy[t] = py; nxq[t] = ux; nyq[t] = uy;
+      wJ[t] = J < 1e-16 ? 0.0 : w[q] * J;
+    }
+  }
+  for (int i = 0; i < g.nt; ++i) {
+    const V2 pf{g.px[i], g.py[i]};
+    double aF = 0.0, aD = 0.0;
+    for (int e = 0; e < g.ne; ++e) {
+      V2 xg[16];
+      for (int q = 0; q < nn; ++q) xg[q] = V2{g.px[e * nn + q], g.py[e * nn + q]};
+      const bool on = (i >= e * nn && i < (e + 1) * nn);
+      if (!on && !near_element(pf, xg, nn, g.elen[e], near_factor)) continue;
+      for (int q = 0; q < npg; ++q) {
+        const int t = e * npg + q;
+        if (wJ[t] == 0) continue;
+        const double rx = yx[t] - pf.x, ry = yy[t] - pf.y;
+        const double R = std::sqrt(rx * rx + ry * ry);
+        if (R < 1e-14) continue;
+        const double wJn = wJ[t] * ((nxq[t] * rx + nyq[t] * ry) / (R * R));
+        aF += dibem_phi_int(rbf, R, k, epsa) * wJn;
+        aD += dibem_rad_id(R, k) * wJn;
+      }
+    }
+    IF[i] += aF;
+    ID[i] += aD;
+  }
+  return 0;
+}
+
 // interior_laplace (src/Laplace/Lubrication.jl:399-416): potential at m
 // interior points, every element through integrate_element.
 int orc_interior_laplace(const OrcGeom* og, double k, int npg, int nearfield, const double* T,

@@ -80,6 +80,8 @@ def lib():
         _lib.orc_dibem_ifid2d.argtypes = [ctypes.POINTER(OrcGeom), d, i, d, d, P, P]
         _lib.orc_dibem_ifid2d.restype = i
         _lib.orc_cr_fn.argtypes = [i, P, i, P]
+        _lib.orc_dibem_ifid_near2d.argtypes = [ctypes.POINTER(OrcGeom), d, i, d, d, i, P, P]
+        _lib.orc_dibem_ifid_near2d.restype = i
         _lib.orc_near_rule.argtypes = [ctypes.POINTER(OrcGeom), i, i, i, d, d, P, P, P]
         _lib.orc_near_rule.restype = i
     return _lib
@@ -264,6 +266,17 @@ def discretize(cad, p):
     normal = np.stack([dx[..., 1] / J, -dx[..., 0] / J], axis=-1)
     L = np.abs(J @ w)
     return nodes, normal, J, L, w
+
+
+def dibem_ifid_near(dad, IF, ID, rbf=3, epsa=1e-16, near_factor=1.5, npg=16):
+    """Adds the near-pair Gauss-rule correction to IF, ID
+    (`_dibem_correct_near_cpu!`, src/Laplace/DIBEM_GPU.jl:272-300); returns them."""
+    g, keep = make_geom(dad)
+    IF = np.array(IF, dtype=np.float64)
+    ID = np.array(ID, dtype=np.float64)
+    lib().orc_dibem_ifid_near2d(ctypes.byref(g), float(dad.properties.k), int(rbf), float(epsa),
+                                float(near_factor), int(npg), _p(IF), _p(ID))
+    return IF, ID
 
 
 def interior_laplace(dad, pts, npg=16, nearfield="tanp3c", T=None, q=None):
