@@ -23,6 +23,7 @@ BEM_OPT_WAIT_LIMIT = 6
 BEM_OPT_INJECT = 7
 BEM_OPT_NEARFIELD = 8
 BEM_OPT_SINGULAR = 9
+BEM_OPT_TC_RESERVE = 10
 NEARFIELD = {"tanp3c": 0, "plain": 1, "tangent": 5, "p3c": 6}
 BEM_NOALLOC_MAX_NT, BEM_NOALLOC_MAX_NE = 16384, 8192
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
@@ -96,6 +97,7 @@ def load(build_if_missing: bool = False):
                               ctypes.POINTER(BemSolveStats)], ctypes.c_int),
         "bem_ctx_set_option": ([ctx_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "bem_selftest": ([ctx_p, ctypes.c_int, ctypes.c_int, PD], ctypes.c_int),
+        "bem_kernel_trace": ([ctx_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), PD, PD], ctypes.c_int),
         "bem_kernel_times": ([ctx_p, PD, ctypes.POINTER(I64), ctypes.c_int], ctypes.c_int),
         "bem_launch_count": ([], I64),
         "bem_dibem_ifid2d": ([ctx_p, ctypes.POINTER(BemGeom2D), D, ctypes.c_int, D, D, ctypes.c_int, ctypes.c_int,
@@ -170,6 +172,18 @@ class Context:
         self.check(self.L.bem_kernel_times(self.h, ms, cnt, n), "kernel_times")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
 
+    def kernel_trace(self, cap: int = 65536):
+        """[(class, start ms, end ms)] of the timed kernel classes since the
+        last call (needs BEM_OPT_KERNEL_TIMING)."""
+        cls = (ctypes.c_int * cap)()
+        t0 = (ctypes.c_double * cap)()
+        t1 = (ctypes.c_double * cap)()
+        n = self.L.bem_kernel_trace(self.h, cap, cls, t0, t1)
+        if n < 0:
+            self.check(-n, "kernel_trace")
+        return [(KERNEL_CLASSES[cls[i]] if cls[i] < len(KERNEL_CLASSES) else cls[i], t0[i], t1[i])
+                for i in range(n)]
+
     def launch_count(self) -> int:
         return int(self.L.bem_launch_count())
 
@@ -179,6 +193,14 @@ class Context:
         out = (ctypes.c_double * 4)()
         self.check(self.L.bem_selftest(self.h, 3, n, out), "selftest")
         return out[0], out[1], out[2]
+
+    def selftest_bulk_compare(self, n: int):
+        """Persistent vs per-tile bulk update on the same operands (needs
+        BEM_OPT_TCGEN05 = 2): (max |diff|, max |entry|) for the whole trailing
+        matrix, then for its part past the first block row and column."""
+        out = (ctypes.c_double * 4)()
+        self.check(self.L.bem_selftest(self.h, 4, n, out), "selftest")
+        return tuple(out)
 
     def selftest_diag(self, n: int = 128):
         """Blocked vs Gauss-Jordan factorization of one 128 x 128 block:

@@ -31,6 +31,7 @@ int ensure_workers(bem_ctx* c, int w) {
   }
   for (bem_ctx* s : c->workers) {
     s->opt_tcgen05 = c->opt_tcgen05;
+    s->opt_tc_reserve = c->opt_tc_reserve;
     s->opt_far_df = c->opt_far_df;
     s->opt_pivot_fallback = c->opt_pivot_fallback;
     s->opt_wait_limit = c->opt_wait_limit;

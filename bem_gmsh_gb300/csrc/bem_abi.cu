@@ -562,4 +562,17 @@ extern "C" int bem_kernel_times(bem_ctx* c, double* ms, int64_t* counts, int n) 
   return BEM_OK;
 }
 
+extern "C" int bem_kernel_trace(bem_ctx* c, int cap, int* cls, double* t0, double* t1) {
+  if (!c || cap < 0) return -BEM_ERR_INVALID;
+  c->prof.collect();
+  const int n = (int)c->prof.trace.size() < cap ? (int)c->prof.trace.size() : cap;
+  for (int i = 0; i < n; ++i) {
+    if (cls) cls[i] = c->prof.trace[i].cls;
+    if (t0) t0[i] = c->prof.trace[i].t0;
+    if (t1) t1[i] = c->prof.trace[i].t1;
+  }
+  c->prof.trace.clear();
+  return n;
+}
+
 extern "C" int64_t bem_launch_count(void) { return (int64_t)bem::g_launches.load(); }

@@ -70,9 +70,14 @@ struct TcPlan {
   alignas(64) unsigned char mAlo[128];
   alignas(64) unsigned char mB[128];
   alignas(64) unsigned char mBlo[128];
+  alignas(64) unsigned char mC[128];  // the matrix as C (persistent kernel)
   bool ok = false;
+  int variant = 1;  // 1: one CTA per tile; 2: persistent, warp-specialized
+  int grid = 0;     // persistent kernel: CTAs (SMs) it may use
 };
-bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, float* Ulo);
+// variant 2 runs the persistent kernel on all SMs but `reserve`
+bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, float* Ulo, int variant = 1,
+             int reserve = 0);
 // Lt, Ltlo, Ulo of step k (from the factored panels)
 void tc_split(const TcPlan& p, int k, cudaStream_t st);
 // part of step k's trailing update: rows [ro, ro+M), columns [co, co+N) of

@@ -34,6 +34,13 @@ struct KProf {
   std::vector<cudaEvent_t> pool;
   double ms[KC_COUNT] = {0};
   long long n[KC_COUNT] = {0};
+  // timeline of the collected records: class, start and end in ms from the
+  // start of the first record of each collection
+  struct Span {
+    int cls;
+    double t0, t1;
+  };
+  std::vector<Span> trace;
 
   cudaEvent_t ev() {
     if (!pool.empty()) {
@@ -64,6 +71,9 @@ struct KProf {
       if (cudaEventElapsedTime(&v, r.a, r.b) == cudaSuccess) {
         ms[r.cls] += v;
         n[r.cls] += 1;
+        float s0 = 0.f;
+        if (trace.size() < (1u << 16) && cudaEventElapsedTime(&s0, pending[0].a, r.a) == cudaSuccess)
+          trace.push_back({r.cls, (double)s0, (double)s0 + v});
       }
       pool.push_back(r.a);
       pool.push_back(r.b);

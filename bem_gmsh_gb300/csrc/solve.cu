@@ -172,7 +172,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
       float* Ltlo = (float*)c->get(bem_ctx::SLOT_TC1 + 3 * h, sizeof(float) * (size_t)Npad * LU_NB);
       float* Ulo = (float*)c->get(bem_ctx::SLOT_TC2 + 3 * h, sizeof(float) * (size_t)Npad * LU_NB);
       if (!Lt || !Ltlo || !Ulo) return BEM_ERR_NOMEM;
-      bem::tc_plan(tcp[h], A32, Npad, Npad, Lt, Ltlo, Ulo);
+      bem::tc_plan(tcp[h], A32, Npad, Npad, Lt, Ltlo, Ulo, c->opt_tcgen05, c->opt_tc_reserve);
     }
   }
   const bool lookahead = use_tc && tcp[0].ok && tcp[1].ok;
@@ -199,7 +199,8 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   // fixed at capture, hence the key.
   const std::vector<const void*> key = {A64, (const void*)(intptr_t)lda, (const void*)(intptr_t)N, A32, cs, Dinv,
                                         Mc, info, tcp[0].Lt, tcp[0].Ltlo, tcp[0].Ulo, tcp[1].Lt, tcp[1].Ltlo,
-                                        tcp[1].Ulo, st, (const void*)(intptr_t)lookahead};
+                                        tcp[1].Ulo, st, (const void*)(intptr_t)lookahead,
+                                        (const void*)(intptr_t)tcp[0].variant, (const void*)(intptr_t)tcp[0].grid};
   const bool graphs = c->opt_graphs && lookahead && !c->prof.on;
   if (graphs && c->lu_graph_key != key) {
     if (c->lu_graph) cudaGraphExecDestroy(c->lu_graph);
@@ -572,7 +573,13 @@ extern "C" int bem_solve2d(bem_ctx* c, const bem_geom2d* g, int kind, double prm
 extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   if (!c) return BEM_ERR_INVALID;
   if (option == BEM_OPT_TCGEN05) {
-    c->opt_tcgen05 = value ? 1 : 0;
+    if (value < 0 || value > 2) return BEM_ERR_INVALID;
+    c->opt_tcgen05 = value;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_TC_RESERVE) {
+    if (value < 0 || value > 64) return BEM_ERR_INVALID;
+    c->opt_tc_reserve = value;
     return BEM_OK;
   }
   if (option == BEM_OPT_KERNEL_TIMING) {
@@ -650,9 +657,9 @@ __global__ void k_maxdiff(const float* A, const float* B, int64_t cnt, float* ou
 // with the legacy mma.sync ones; out[0] = max |difference of the factors|,
 // out[1] = max |factor|, out[2] / out[3] = factor times (ms) tcgen05 / legacy.
 extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
-  if (!c || !out || which < 1 || which > 3 || n < LU_NB || n % LU_NB != 0 || n > 16384)
+  if (!c || !out || which < 1 || which > 4 || n < LU_NB || n % LU_NB != 0 || n > 16384)
     return BEM_ERR_INVALID;
-  if (which == 3 && n < 2 * LU_NB) return BEM_ERR_INVALID;
+  if ((which == 3 || which == 4) && n < 2 * LU_NB) return BEM_ERR_INVALID;
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
   if (which == 3) {
@@ -665,7 +672,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
     int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
     if (!A1 || !Lt || !Ltlo || !Ulo || !info) return BEM_ERR_NOMEM;
     bem::TcPlan tcp;
-    if (!bem::tc_plan(tcp, A1, n, n, Lt, Ltlo, Ulo)) {
+    if (!bem::tc_plan(tcp, A1, n, n, Lt, Ltlo, Ulo, c->opt_tcgen05, c->opt_tc_reserve)) {
       c->last_error = "tensor map encoding failed";
       return BEM_ERR_UNSUPPORTED;
     }
@@ -691,6 +698,53 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
     out[1] = 8.0 * (double)rem * rem / (ms * 1e-3) / 1e9;
     out[2] = 3.0 * 2.0 * (double)rem * rem * LU_NB / (ms * 1e-3) / 1e12;
     out[3] = 0.0;
+    return BEM_OK;
+  }
+  if (which == 4) {
+    // the two bulk-update kernels on the same operands: step 0's update of
+    // the whole trailing matrix and, on a second copy, of its part past the
+    // first block row and column (the look-ahead's shape); out[0] / out[1] =
+    // max |difference| / max |entry| of the two results, out[2] / out[3] =
+    // the same for the second shape
+    if (c->opt_tcgen05 != 2) return BEM_ERR_INVALID;
+    float* A1 = (float*)c->get(bem_ctx::SLOT_TEST0, sizeof(float) * (size_t)n * n);
+    float* A2 = (float*)c->get(bem_ctx::SLOT_TEST1, sizeof(float) * (size_t)n * n);
+    float* Lt = (float*)c->get(bem_ctx::SLOT_TC0, sizeof(float) * (size_t)n * LU_NB);
+    float* Ltlo = (float*)c->get(bem_ctx::SLOT_TC1, sizeof(float) * (size_t)n * LU_NB);
+    float* Ulo = (float*)c->get(bem_ctx::SLOT_TC2, sizeof(float) * (size_t)n * LU_NB);
+    int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
+    if (!A1 || !A2 || !Lt || !Ltlo || !Ulo || !info) return BEM_ERR_NOMEM;
+    bem::TcPlan p1, p2;
+    if (!bem::tc_plan(p1, A1, n, n, Lt, Ltlo, Ulo, 1, 0) ||
+        !bem::tc_plan(p2, A2, n, n, Lt, Ltlo, Ulo, 2, c->opt_tc_reserve) || p2.variant != 2) {
+      c->last_error = "tensor map encoding failed";
+      return BEM_ERR_UNSUPPORTED;
+    }
+    const int rem = n - LU_NB;
+    float* d = (float*)(info + 8);
+    float h[4];
+    cudaMemsetAsync(info, 0, 16, st);
+    cudaMemsetAsync(d, 0, 16, st);
+    for (int shape = 0; shape < 2; ++shape) {
+      const int o = shape ? LU_NB : 0;
+      if (rem - o <= 0) break;
+      k_fill_test<<<1024, 256, 0, st>>>(A1, n, n, 999u + shape);
+      cudaMemcpyAsync(A2, A1, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, st);
+      bem::tc_split(p1, 0, st);
+      bem::tc_gemm_sub(p1, 0, o, o, rem - o, rem - o, info + 1, st);
+      bem::tc_gemm_sub(p2, 0, o, o, rem - o, rem - o, info + 1, st);
+      k_maxdiff<<<512, 256, 0, st>>>(A1, A2, (int64_t)n * n, d + 2 * shape);
+    }
+    int herr = 0;
+    cudaMemcpyAsync(h, d, 16, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&herr, info + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return c->cuda_fail(e, "selftest bulk kernels");
+    if (herr) {
+      c->last_error = "bulk update reported a barrier timeout";
+      return BEM_ERR_CUDA;
+    }
+    for (int i = 0; i < 4; ++i) out[i] = h[i];
     return BEM_OK;
   }
   if (which == 2) {
@@ -731,7 +785,8 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
   float* Ltlo2 = (float*)c->get(bem_ctx::SLOT_TC4, sizeof(float) * (size_t)n * LU_NB);
   float* Ulo2 = (float*)c->get(bem_ctx::SLOT_TC5, sizeof(float) * (size_t)n * LU_NB);
   if (!Lt2 || !Ltlo2 || !Ulo2 || !c->lookahead_ready(K)) return BEM_ERR_NOMEM;
-  if (!bem::tc_plan(tcp[0], A1, n, n, Lt, Ltlo, Ulo) || !bem::tc_plan(tcp[1], A1, n, n, Lt2, Ltlo2, Ulo2)) {
+  if (!bem::tc_plan(tcp[0], A1, n, n, Lt, Ltlo, Ulo, c->opt_tcgen05, c->opt_tc_reserve) ||
+      !bem::tc_plan(tcp[1], A1, n, n, Lt2, Ltlo2, Ulo2, c->opt_tcgen05, c->opt_tc_reserve)) {
     c->last_error = "tensor map encoding failed";
     return BEM_ERR_UNSUPPORTED;
   }

@@ -132,12 +132,13 @@ def cpu_reference(dad_factory, steps, warmup, npg):
     return ts, x, stages
 
 
-# DRAM traffic of one bulk trailing update (k_gemm_tc) at the C2 trailing size,
-# from one ncu capture of the update timed alone (bem_selftest which = 3,
-# n = 8192, trailing block 8064^2): dram__bytes_read 276831744 B +
-# dram__bytes_write 199586048 B for 8 * 8064^2 = 520224768 algorithmic bytes.
-GEMM_TRAFFIC_CAPTURE = {"launch": "bulk update alone, trailing block 8064^2", "read_bytes": 276831744,
-                        "write_bytes": 199586048, "algorithmic_bytes": 8 * 8064 ** 2}
+# DRAM traffic of one bulk trailing update (k_gemm_tc_p, the persistent
+# kernel) at the C2 trailing size, from one ncu capture of the update timed
+# alone (bem_selftest which = 3, n = 8192, trailing block 8064^2):
+# dram__bytes_read 276934400 B + dram__bytes_write 200425984 B for
+# 8 * 8064^2 = 520224768 algorithmic bytes.
+GEMM_TRAFFIC_CAPTURE = {"launch": "bulk update alone, trailing block 8064^2", "read_bytes": 276934400,
+                        "write_bytes": 200425984, "algorithmic_bytes": 8 * 8064 ** 2}
 
 
 def extra_configs(ctx):
@@ -501,7 +502,7 @@ def main():
         # per step, 8 rem'^2 B (3xTF32 intensity 96 flop/B is below the TF32
         # machine balance, so HBM bounds it); operands come from L2
         "lu_trail": ("hbm", sum(8.0 * max(r - 128, 0) ** 2 for r in rems), "GB/s",
-                     "tcgen05 3xTF32 trailing updates (k_gemm_tc): C read + write per step"),
+                     "tcgen05 3xTF32 trailing updates (k_gemm_tc_p): C read + write per step"),
         # bytes: FP32 L and U read once per preconditioner application
         "trsv": ("hbm", 4.0 * nb * nb * iters_last, "GB/s", "FP32 LU read per sweep pair"),
         # bytes: one FP64 A read per product (one per iteration + the final
@@ -525,7 +526,7 @@ def main():
     cap = GEMM_TRAFFIC_CAPTURE
     ratio = (cap["read_bytes"] + cap["write_bytes"]) / cap["algorithmic_bytes"]
     nbulk = max(1, sum(1 for r in rems if r > 128))
-    roof.update({"kernel": "k_gemm_tc (bulk trailing update)", "kernel_class": dom,
+    roof.update({"kernel": "k_gemm_tc_p (persistent bulk trailing update)", "kernel_class": dom,
                  "traffic": ratio * algo["lu_trail"][1] / nbulk,
                  "traffic_note": "bytes per average bulk launch: the measured DRAM read+write / algorithmic "
                                  "ratio of one full-size ncu capture (%s, %.3f) times the algorithmic bytes "

@@ -45,7 +45,9 @@ extern "C" {
 #define BEM_MEM_DEVICE 1
 
 /* context options (bem_ctx_set_option) */
-#define BEM_OPT_TCGEN05 1       /* 1 (default): LU trailing updates on tcgen05; 0: legacy mma.sync */
+#define BEM_OPT_TCGEN05 1       /* LU trailing updates: 2 (default) a persistent warp-specialized tcgen05
+                                   kernel (TMEM double buffer, C through TMA); 1 tcgen05, one CTA per
+                                   tile; 0 legacy mma.sync */
 #define BEM_OPT_KERNEL_TIMING 2 /* 1: time kernel classes with CUDA events (bem_kernel_times) */
 #define BEM_OPT_FAR_DF 3        /* far-field Laplace entries of FP64 systems evaluated in double-float
                                    (FP32 pairs, ~1e-14 relative): 0 never, 1 (default) in mixed-precision
@@ -76,6 +78,8 @@ extern "C" {
 #define BEM_OPT_SINGULAR 9      /* on-element rule, the reference's `singular` knob
                                    (src/Core/Assembly_full.jl:282-283): 0 (default) interpolated
                                    Guiggiani, 1 Telles cubic map of the npg Gauss rule */
+#define BEM_OPT_TC_RESERVE 10   /* SMs the persistent trailing-update kernel (BEM_OPT_TCGEN05 = 2) leaves
+                                   to the look-ahead's diagonal and panel kernels (default 8, <= 64) */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */
@@ -223,6 +227,15 @@ int bem_ctx_set_option(bem_ctx* ctx, int option, int value);
  * (BEM_KC_*) since the last call, with BEM_OPT_KERNEL_TIMING on; resets the
  * accumulators.  Tracing facility, no reference counterpart. */
 int bem_kernel_times(bem_ctx* ctx, double* ms, int64_t* counts, int n);
+
+/*
+ * Timeline of the timed kernel classes (BEM_OPT_KERNEL_TIMING on) since the
+ * last call: up to cap records of (class, start ms, end ms), times from the
+ * start of the first record of each synchronisation window, in launch order
+ * per stream.  Returns the number of records (negative status on error) and
+ * clears the timeline.  No reference counterpart (instrumentation).
+ */
+int bem_kernel_trace(bem_ctx* ctx, int cap, int* cls, double* t0_ms, double* t1_ms);
 
 /* Number of kernel launches made by the library in this process. */
 int64_t bem_launch_count(void);
@@ -411,6 +424,10 @@ int bem_strain_stress2d(bem_ctx* ctx, const bem_geom2d* geom, double lam, double
  * which = 3: the bulk trailing update of one LU step, C ((n-128)^2) -= L U,
  * timed alone: out[0] ms per launch, out[1] algorithmic GB/s (C read and
  * write), out[2] TF32 tensor TFLOP/s (three products).  n >= 256.
+ * which = 4 (BEM_OPT_TCGEN05 = 2): the persistent and the per-tile bulk
+ * update on the same operands, over the whole trailing matrix and over its
+ * part past the first block row and column; out[0], out[1] = max |difference|,
+ * max |entry| of the first shape, out[2], out[3] the same for the second.
  */
 int bem_selftest(bem_ctx* ctx, int which, int n, double* out);
 

@@ -119,6 +119,41 @@ def test_lu_building_blocks():
     assert r[0] / r[1] < 1e-5, r
 
 
+@pytest.mark.parametrize("n", [384, 512, 2048, 4096])
+def test_persistent_bulk_update_matches_per_tile_kernel(n):
+    """The persistent warp-specialized tcgen05 update (TMEM double buffer,
+    C through TMA, several tiles per CTA at n = 4096) against the one-CTA-per-
+    tile kernel on the same operands, for the whole trailing matrix and for
+    the look-ahead's shape (past the first block row and column, a half tile
+    at the last column at n = 384 and 512): the same MMA sequence and the same
+    epilogue formula, so the results agree to FP32 rounding of the epilogue
+    (bit-identical in practice)."""
+    from bem_gmsh_gb300 import _lib
+    ctx = _lib.Context()
+    try:
+        ctx.set_option(_lib.BEM_OPT_TCGEN05, 2)
+        for reserve in (0, 8):
+            ctx.set_option(_lib.BEM_OPT_TC_RESERVE, reserve)
+            r = ctx.selftest_bulk_compare(n)
+            assert r[0] <= 1e-6 * r[1] and r[2] <= 1e-6 * r[3], r
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_lu_with_each_bulk_kernel(variant):
+    """The look-ahead LU with either tcgen05 bulk-update kernel agrees with the
+    legacy mma.sync factorization to FP32 rounding."""
+    from bem_gmsh_gb300 import _lib
+    ctx = _lib.Context()
+    try:
+        ctx.set_option(_lib.BEM_OPT_TCGEN05, variant)
+        r = ctx.selftest_lu(2048)
+        assert r[0] / r[1] < 1e-5, r
+    finally:
+        ctx.close()
+
+
 def test_factorization_graph_replay_matches_direct_launches():
     """The mixed solve captures its factorization in a CUDA graph on the
     second call with unchanged buffers and replays it afterwards; replayed
