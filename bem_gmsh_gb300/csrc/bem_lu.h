@@ -27,13 +27,17 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
 // M_b couplings of the triangular sweeps (Mc: K * 2 * 128^2 floats), after
 // the factorization
 void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float* Mc, cudaStream_t st);
+// (epoch, value) words of the triangular sweeps: y of both sweeps (2 Npad)
+// and the helpers' partial sums (at most LU_TRSV_PMAX CTAs per block row)
+constexpr int LU_TRSV_PMAX = 4;
+inline size_t lu_tag_words(int Npad) { return (size_t)(2 + 2 * LU_TRSV_PMAX) * (size_t)Npad; }
 // out <- U^{-1} L^{-1} r on padded FP32 vectors.  tmp: Npad floats (the
-// forward result); tags: 2 Npad words of (epoch, value) scratch, zeroed
-// before the first call; epoch: > 0 and different in every call on the same
-// tags; err: timeout flag, set when a wait polled wait_limit times in vain.
-// wepoch_shift (failure injection, normally 0): results are published under
-// epoch + wepoch_shift, so that a nonzero shift makes every dependent wait
-// run out.  r may be clobbered.  Returns 0 or a CUDA error.
+// forward result); tags: lu_tag_words(Npad) words of (epoch, value) scratch,
+// zeroed before the first call; epoch: > 0 and different in every call on
+// the same tags; err: timeout flag, set when a wait polled wait_limit times
+// in vain.  wepoch_shift (failure injection, normally 0): results are
+// published under epoch + wepoch_shift, so that a nonzero shift makes every
+// dependent wait run out.  r may be clobbered.  Returns 0 or a CUDA error.
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st,
                  int wait_limit = 1 << 20, int wepoch_shift = 0);
@@ -81,10 +85,14 @@ bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, 
 // Lt, Ltlo, Ulo of step k (from the factored panels)
 void tc_split(const TcPlan& p, int k, cudaStream_t st);
 // part of step k's trailing update: rows [ro, ro+M), columns [co, co+N) of
-// the trailing matrix  A22 -= L21 U12
-int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st);
+// the trailing matrix  A22 -= L21 U12.  ctr: two zeroed device ints that the
+// persistent kernel's CTAs claim tiles from (and rearm when done), or null
+// for a static tile order; launches sharing ctr must not overlap.
+int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st,
+                int* ctr = nullptr);
+// ctr: two zeroed device ints for the bulk updates' tile counter (or null)
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err);
+                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err, int* ctr = nullptr);
 
 }  // namespace bem

@@ -149,6 +149,8 @@ struct TcArgs {
   float alpha, beta;
   int* err;
   int cx0, cy0;   // C map (persistent kernel): row and column of C(0, 0)
+  int* ctr;       // persistent kernel: {next tile, CTAs done} (zero at launch),
+                  // or null for the static order t = blockIdx.x + i gridDim.x
 };
 
 __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_gemm_tc(const __grid_constant__ CUtensorMap mA,
@@ -413,6 +415,19 @@ __device__ __forceinline__ int pwait_warp(uint32_t bar, uint32_t parity, volatil
   return ok;
 }
 
+// one consumer thread's next tile from the CTA's tile ring (P_TRING slots
+// written by the operand producer): the tile, or -1 at the end or after a
+// failure; the slot is released at once
+constexpr int P_TRING = 4;
+__device__ __forceinline__ int take_tile(uint32_t tile_full, uint32_t tile_empty, volatile int* s_tile, int it,
+                                         volatile int* fail) {
+  const int slot = it % P_TRING;
+  if (!pwait(tile_full + 8 * slot, (it / P_TRING) & 1, fail)) return -1;
+  const int t = s_tile[slot];
+  mbar_arrive(tile_empty + 8 * slot);
+  return t;
+}
+
 __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constant__ CUtensorMap mA,
                                                           const __grid_constant__ CUtensorMap mAlo,
                                                           const __grid_constant__ CUtensorMap mB,
@@ -424,17 +439,22 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
   const uint32_t cbuf0 = tiles + P_STAGES * STAGE_BYTES;
   uint8_t* misc = dsm + (tiles - base_u) + P_STAGES * STAGE_BYTES + P_CBUF * P_CBYTES;
   // barriers: op_full[P_STAGES], op_empty[P_STAGES], acc_full[2],
-  // acc_empty[2], c_full[P_CBUF], c_empty[P_CBUF], fin
-  constexpr int NBAR = 2 * P_STAGES + 4 + 2 * P_CBUF + 1;
+  // acc_empty[2], c_full[P_CBUF], c_empty[P_CBUF], fin, tile_full[P_TRING],
+  // tile_empty[P_TRING]
+  constexpr int NBAR = 2 * P_STAGES + 4 + 2 * P_CBUF + 1 + 2 * P_TRING;
   uint64_t* bars = (uint64_t*)misc;
   const uint32_t op_full = smem_u32(&bars[0]), op_empty = smem_u32(&bars[P_STAGES]);
   const uint32_t acc_full = smem_u32(&bars[2 * P_STAGES]), acc_empty = acc_full + 16;
   const uint32_t c_full = acc_empty + 16, c_empty = c_full + 8 * P_CBUF, fin = c_empty + 8 * P_CBUF;
+  const uint32_t tile_full = fin + 8, tile_empty = tile_full + 8 * P_TRING;
   uint32_t* s_tmem = (uint32_t*)(misc + 8 * NBAR);
   volatile int* s_fail = (volatile int*)(misc + 8 * NBAR + 4);
   // [0] operand chunks issued, [1] C chunks issued, [2] operand chunks
   // consumed, [3] C chunks consumed (for the exit path)
   volatile int* s_cnt = (volatile int*)(misc + 8 * NBAR + 8);
+  // the tile ring and the epilogue's current tile
+  volatile int* s_tile = (volatile int*)(misc + 8 * NBAR + 24);
+  volatile int* s_etile = (volatile int*)(misc + 8 * NBAR + 24 + 4 * P_TRING);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int MT = a.M / BM, NT = (a.N + BN - 1) / BN, T = MT * NT;
 
@@ -452,6 +472,10 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
       mbar_init(c_empty + 8 * i, 1);
     }
     mbar_init(fin, 1);
+    for (int i = 0; i < P_TRING; ++i) {
+      mbar_init(tile_full + 8 * i, 1);
+      mbar_init(tile_empty + 8 * i, 3);  // MMA issuer, C producer, epilogue
+    }
     *s_fail = 0;
     for (int i = 0; i < 4; ++i) s_cnt[i] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -469,9 +493,18 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
   constexpr int NCH = LU_NB / BK;
 
   if (warp == 0 && lane == 0) {
-    // operand producer
+    // operand producer; it also claims the tiles (from the global counter
+    // when there is one, so that CTAs that start late take fewer tiles)
+    // and hands them to the other roles through the tile ring
     int opc = 0;
-    for (int t = blockIdx.x; t < T && !*s_fail; t += gridDim.x) {
+    for (int it = 0;; ++it) {
+      int t = a.ctr ? atomicAdd(a.ctr, 1) : (int)blockIdx.x + it * (int)gridDim.x;
+      if (t >= T || *s_fail) t = -1;
+      const int slot = it % P_TRING;
+      if (it >= P_TRING && !pwait(tile_empty + 8 * slot, ((it / P_TRING) - 1) & 1, s_fail)) break;
+      s_tile[slot] = t;
+      mbar_arrive(tile_full + 8 * slot);
+      if (t < 0) break;
       const int m0 = (t % MT) * BM, n0 = (t / MT) * BN;
       for (int c = 0; c < NCH && !*s_fail; ++c, ++opc) {
         const int s = opc % P_STAGES;
@@ -488,7 +521,9 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
   } else if (warp == 2 && lane == 0) {
     // C producer
     int cc = 0;
-    for (int t = blockIdx.x; t < T && !*s_fail; t += gridDim.x) {
+    for (int it = 0;; ++it) {
+      const int t = take_tile(tile_full, tile_empty, s_tile, it, s_fail);
+      if (t < 0) break;
       const int m0 = (t % MT) * BM, n0 = (t / MT) * BN;
       const int nch = min(P_NCHUNK, (a.N - n0 + P_CW - 1) / P_CW);
       for (int ch = 0; ch < nch && !*s_fail; ++ch, ++cc) {
@@ -498,11 +533,13 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
         tma_load_2d(cbuf0 + b * P_CBYTES, &mC, a.cx0 + m0, a.cy0 + n0 + ch * P_CW, c_full + 8 * b);
         s_cnt[1] = cc + 1;
       }
+      if (*s_fail) break;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    int opc = 0, it = 0;
-    for (int t = blockIdx.x; t < T && !*s_fail; t += gridDim.x, ++it) {
+    int opc = 0;
+    for (int it = 0;; ++it) {
+      if (take_tile(tile_full, tile_empty, s_tile, it, s_fail) < 0) break;
       const int b = it & 1;
       if (it >= 2 && !pwait(acc_empty + 8 * b, ((it >> 1) - 1) & 1, s_fail)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -536,8 +573,13 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
     // only skips work and no warp is left at a barrier.
     const int quad = warp & 3;
     const int rloc = quad * 32 + lane;
-    int cc = 0, it = 0;
-    for (int t = blockIdx.x; t < T; t += gridDim.x, ++it) {
+    int cc = 0;
+    for (int it = 0;; ++it) {
+      // thread 128 takes the tile for the four warps
+      if (threadIdx.x == 128) *s_etile = take_tile(tile_full, tile_empty, s_tile, it, s_fail);
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      const int t = *s_etile;
+      if (t < 0) break;
       const int m0 = (t % MT) * BM, n0 = (t / MT) * BN;
       const int b = it & 1;
       const int okt = pwait_warp(acc_full + 8 * b, (it >> 1) & 1, s_fail, lane);
@@ -585,6 +627,14 @@ __global__ void __launch_bounds__(P_THREADS, 1) k_gemm_tc_p(const __grid_constan
   }
   __syncwarp();
   __syncthreads();
+  if (threadIdx.x == 0 && a.ctr) {
+    // the last CTA to finish (every claim made) rearms the counter
+    __threadfence();
+    if (atomicAdd(a.ctr + 1, 1) == (int)gridDim.x - 1) {
+      atomicExch(a.ctr, 0);
+      atomicExch(a.ctr + 1, 0);
+    }
+  }
   if (*s_fail) {
     if (threadIdx.x == 0) {
       atomicExch(a.err, 1);
@@ -737,7 +787,7 @@ void tc_split(const TcPlan& p, int k, cudaStream_t st) {
   count_launches(1);
 }
 
-int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st) {
+int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, cudaStream_t st, int* ctr) {
   if (M <= 0 || N <= 0) return 0;
   const int kk = k * LU_NB;
   tc::TcArgs a{};
@@ -760,6 +810,7 @@ int tc_gemm_sub(const TcPlan& p, int k, int ro, int co, int M, int N, int* err, 
   if (p.variant == 2 && (N % tc::P_CW == 0 || cy0 + N == p.Npad)) {
     a.cx0 = kk + LU_NB + ro;
     a.cy0 = cy0;
+    a.ctr = ctr;
     const int T = (M / tc::BM) * ((N + tc::BN - 1) / tc::BN);
     tc::k_gemm_tc_p<<<T < p.grid ? T : p.grid, tc::P_THREADS, tc::P_SMEM, st>>>(
         *(const CUtensorMap*)p.mA, *(const CUtensorMap*)p.mAlo, *(const CUtensorMap*)p.mB,

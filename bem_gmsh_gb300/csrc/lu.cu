@@ -464,10 +464,13 @@ __global__ void k_panel_gemv(const float* __restrict__ P, int64_t ld, int rows,
 // same kernel as k_panel_gemv; kept separate for clarity of the launch sites.
 
 // ---------------------------------------------------------------------------
-// Wavefront triangular solve: one CTA per block row, one launch per sweep.
-// CTA q of the forward sweep computes y_b (b = q) = Linv_b (r_b - sum_{j<b}
-// L_bj y_j); the backward sweep runs b = K-1-q downwards with U and Uinv_b.
-// A CTA waits only for lower-numbered CTAs (flags set with release
+// Wavefront triangular solve: P CTAs per block row, one launch per sweep.
+// Block row q of the forward sweep computes y_b (b = q) = Linv_b (r_b -
+// sum_{j<b} L_bj y_j); the backward sweep runs b = K-1-q downwards with U and
+// Uinv_b.  The non-adjacent sum is split over the block row's P CTAs: P-1
+// helpers sum the earlier blocks and publish their partial sums, the owner
+// sums the latest ones, adds the partials and runs the dependent step.
+// A CTA waits only for blocks solved before its own (flags set with release
 // semantics after their block is written); the waits are bounded and a
 // timeout is reported through `err` instead of hanging.  The launch is
 // cooperative so that all CTAs are resident.
@@ -535,39 +538,49 @@ __global__ void __launch_bounds__(256) k_lu_couplings(const float* __restrict__ 
     *(float4*)&Mo[(size_t)(qc + c0 + j) * LU_NB + qr + r0] = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
 }
 
+// Words per CTA of the partial sums (ptags): 128 (epoch, value) words, P at
+// most TRSV_PMAX CTAs per block row.
 template <bool UPPER>
 __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, int64_t ld, int K,
                                                    const float* __restrict__ Dinv, const float* __restrict__ Mc,
-                                                   const float* r, float* y, unsigned long long* tags, int epoch,
-                                                   int wepoch, int wait_limit, int* err) {
+                                                   const float* r, float* y, unsigned long long* tags,
+                                                   unsigned long long* ptags, int P, int epoch, int wepoch,
+                                                   int wait_limit, int* err) {
   extern __shared__ float Ds[];  // the block's inverse, [col][row], LU_NB * (LU_NB + 1)
   __shared__ float ys[LU_NB];
   __shared__ float part[2][LU_NB];
   __shared__ int bad;
   const int t = threadIdx.x, row = t & (LU_NB - 1), half = t >> 7;
-  const int b = UPPER ? (K - 1 - (int)blockIdx.x) : (int)blockIdx.x;
+  const int bi = (int)blockIdx.x / P, pp = (int)blockIdx.x % P;
+  const bool owner = pp == P - 1;
+  const int b = UPPER ? (K - 1 - bi) : bi;
   const size_t rb = (size_t)b * LU_NB;
-  const float* Db = Dinv + (size_t)b * 2 * LU_NB * LU_NB + (UPPER ? LU_NB * LU_NB : 0);
-  for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
-    int rr = idx & (LU_NB - 1), c = idx >> 7;
-    Ds[c * (LU_NB + 1) + rr] = Db[rr + (size_t)c * LU_NB];
-  }
+  const int nj = UPPER ? (K - 1 - b) : b;  // blocks solved before this one
+  const int noff = nj > 1 ? nj - 1 : 0;    // ... but the adjacent one
+  // this CTA's share of the non-adjacent blocks, in solve order
+  const int s0 = (int)((long long)noff * pp / P), s1 = (int)((long long)noff * (pp + 1) / P);
   if (t == 0) bad = 0;
-  float acc = (half == 0) ? r[rb + row] : 0.f;
-  const int nj = UPPER ? (K - 1 - b) : b;
-  // this thread's half row of the coupling to the adjacent block
   float mreg[LU_NB / 2];
-  if (nj > 0) {
-    const float* Mb = Mc + (size_t)(2 * b + (UPPER ? 1 : 0)) * LU_NB * LU_NB;
+  if (owner) {
+    const float* Db = Dinv + (size_t)b * 2 * LU_NB * LU_NB + (UPPER ? LU_NB * LU_NB : 0);
+    for (int idx = t; idx < LU_NB * LU_NB; idx += blockDim.x) {
+      int rr = idx & (LU_NB - 1), c = idx >> 7;
+      Ds[c * (LU_NB + 1) + rr] = Db[rr + (size_t)c * LU_NB];
+    }
+    // this thread's half row of the coupling to the adjacent block
+    if (nj > 0) {
+      const float* Mb = Mc + (size_t)(2 * b + (UPPER ? 1 : 0)) * LU_NB * LU_NB;
 #pragma unroll
-    for (int q = 0; q < LU_NB / 2; ++q) mreg[q] = Mb[(size_t)(half * (LU_NB / 2) + q) * LU_NB + row];
+      for (int q = 0; q < LU_NB / 2; ++q) mreg[q] = Mb[(size_t)(half * (LU_NB / 2) + q) * LU_NB + row];
+    }
   }
+  float acc = (owner && half == 0) ? r[rb + row] : 0.f;
   __syncthreads();
-  // waits for y_j: each of the first 128 threads polls its own (epoch, value)
-  // word; false when the wait ran out
-  auto fetch = [&](int j) {
+  // waits for the 128 (epoch, value) words at w: each of the first 128
+  // threads polls its own word; false when the wait ran out
+  auto fetch = [&](const unsigned long long* w0) {
     if (t < LU_NB) {
-      const unsigned long long* w = tags + (size_t)j * LU_NB + t;
+      const unsigned long long* w = w0 + t;
       unsigned long long v = ld_acquire_u64(w);
       int it = 0;
       while ((int)(v >> 32) != epoch) {
@@ -583,26 +596,69 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     __syncthreads();
     return bad == 0;
   };
-  // every solved block but the adjacent one
-  for (int s = 0; s + 1 < nj; ++s) {
-    const int j = UPPER ? (K - 1 - s) : s;
-    // prefetch this thread's 64 coefficients of block (b, j) before waiting
-    float pre[LU_NB / 2];
-    const float* P = A + (rb + row) + ((size_t)j * LU_NB + half * (LU_NB / 2)) * ld;
+  auto blk = [&](int s) { return UPPER ? (K - 1 - s) : s; };
+  // this thread's 64 coefficients of block (b, j): row `row`, columns
+  // half * 64 .. + 63 (coalesced across the warp)
+  auto coef = [&](int s) { return A + (rb + row) + ((size_t)blk(s) * LU_NB + half * (LU_NB / 2)) * ld; };
+  // non-adjacent blocks, two register buffers: block s+1's coefficients
+  // load while block s waits for its y and is applied
+  {
+    float pa[LU_NB / 2], pb[LU_NB / 2];
+    int s = s0;
+    if (s < s1) {
+      const float* P0 = coef(s);
 #pragma unroll
-    for (int q = 0; q < LU_NB / 2; ++q) pre[q] = P[(size_t)q * ld];
-    if (!fetch(j)) {
+      for (int q = 0; q < LU_NB / 2; ++q) pa[q] = P0[(size_t)q * ld];
+    }
+    while (s < s1) {
+      if (s + 1 < s1) {
+        const float* P1 = coef(s + 1);
+#pragma unroll
+        for (int q = 0; q < LU_NB / 2; ++q) pb[q] = P1[(size_t)q * ld];
+      }
+      if (!fetch(tags + (size_t)blk(s) * LU_NB)) {
+        if (t == 0) atomicExch(err, 1);
+        return;
+      }
+#pragma unroll
+      for (int q = 0; q < LU_NB / 2; ++q) acc -= pa[q] * ys[half * (LU_NB / 2) + q];
+      __syncthreads();
+      if (++s >= s1) break;
+      if (s + 1 < s1) {
+        const float* P1 = coef(s + 1);
+#pragma unroll
+        for (int q = 0; q < LU_NB / 2; ++q) pa[q] = P1[(size_t)q * ld];
+      }
+      if (!fetch(tags + (size_t)blk(s) * LU_NB)) {
+        if (t == 0) atomicExch(err, 1);
+        return;
+      }
+#pragma unroll
+      for (int q = 0; q < LU_NB / 2; ++q) acc -= pb[q] * ys[half * (LU_NB / 2) + q];
+      __syncthreads();
+      ++s;
+    }
+  }
+  part[half][row] = acc;
+  __syncthreads();
+  unsigned long long* pw = ptags + (size_t)(b * P + pp) * LU_NB;
+  if (!owner) {
+    // a helper publishes its partial sum (0 for an empty share)
+    if (t < LU_NB)
+      st_relaxed_u64(pw + t, ((unsigned long long)(unsigned)wepoch << 32) | __float_as_uint(part[0][t] + part[1][t]));
+    return;
+  }
+  float sum = (t < LU_NB) ? part[0][t] + part[1][t] : 0.f;
+  for (int q = 0; q + 1 < P; ++q) {
+    if (!fetch(ptags + (size_t)(b * P + q) * LU_NB)) {
       if (t == 0) atomicExch(err, 1);
       return;
     }
-#pragma unroll
-    for (int q = 0; q < LU_NB / 2; ++q) acc -= pre[q] * ys[half * (LU_NB / 2) + q];
+    if (t < LU_NB) sum += ys[t];
     __syncthreads();
   }
   // z_b = D_b (r_b - ...)
-  part[half][row] = acc;
-  __syncthreads();
-  if (t < LU_NB) ys[t] = part[0][t] + part[1][t];
+  if (t < LU_NB) ys[t] = sum;
   __syncthreads();
   float o0 = 0.f, o1 = 0.f;
 #pragma unroll 16
@@ -616,7 +672,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
   if (nj > 0) {
     // y_b = z_b - M_b y_adjacent
     __syncthreads();  // part and ys are reused
-    if (!fetch(UPPER ? b + 1 : b - 1)) {
+    if (!fetch(tags + (size_t)(UPPER ? b + 1 : b - 1) * LU_NB)) {
       if (t == 0) atomicExch(err, 1);
       return;
     }
@@ -761,24 +817,20 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 //      16 x 16 block.  Column block p of L\U and both sub-block inverses are
 //      final and are written out.
 //   C  the trailing update A22 -= L21 U12 on 4 x 4 register tiles.
-// 24 block barriers in all.  With `pre` the block first gets the update of
-// the previous step, A_kk -= L_{k,k-1} U_{k-1,k} (K = 128 in chunks of 32),
-// which the look-ahead otherwise leaves to the thin update, so that the rest
-// of that update runs beside this kernel.  105 KB of shared memory and the
-// whole register file (512 threads x 128): the kernel runs alone on an SM
-// (capped at 64 registers to share an SM with a bulk-update tile it measured
-// 40 % slower).  A and ld must allow 16-byte accesses (ld % 4 == 0, 16-byte
-// aligned A).
+// 24 block barriers in all.  In the look-ahead LU the previous step's update
+// of the block itself comes just before the kernel, as one tile of the
+// tensor-core trailing update (inside this kernel, on mma.sync, it took 12 of
+// its 45 us; the thin update leaves the block out).  70 KB of shared memory
+// and the whole register file (512 threads x 128): the kernel runs alone on
+// an SM (capped at 64 registers to share an SM with a bulk-update tile it
+// measured 40 % slower).  A and ld must allow 16-byte accesses (ld % 4 == 0,
+// 16-byte aligned A).
 // ---------------------------------------------------------------------------
 constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
 // shared floats of the diagonal kernel: L\U, four double-buffered pivot
-// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses,
-// the operand chunks of the pre-update (L 128 x 32, U 32 x 128)
-constexpr int PRE_KC = 32;
-constexpr int PRE_ULD = PRE_KC + 4;
-constexpr int DIAG_SMEM =
-    (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 4 * DB * DB + PRE_KC * TLD + LU_NB * PRE_ULD);
+// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses
+constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 4 * DB * DB);
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -819,31 +871,13 @@ __device__ __forceinline__ float rcp_nr(float x) {
   return fmaf(r, fmaf(-x, r, 1.f), r);
 }
 
-// x = hi + lo with hi = tf32(x) (round to nearest) and lo = tf32(x - hi)
-__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
-  const float r = x - __uint_as_float(hi);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
-}
-
-// d += a b, one m16n8k8 TF32 tile (A row-major fragment, B column-major)
-__device__ __forceinline__ void mma_tf32_16x8x8(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-      "{%0, %1, %2, %3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
 __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64_t ld, int k,
-                                                 float* __restrict__ SI, int* __restrict__ info, int pre) {
+                                                 float* __restrict__ SI, int* __restrict__ info) {
   extern __shared__ __align__(16) float dsm[];
   float* S = dsm;                       // A -> L\U
   float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
   float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
   float* LiP = Ls + 16 * 20;            // [parity][Linv_pp, Uinv_pp], column-major, ld 16
-  float* Lc = LiP + 4 * DB * DB;        // pre-update L chunk [q][r], ld TLD
-  float* Uc = Lc + PRE_KC * TLD;        // pre-update U chunk [c][q], ld PRE_ULD
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
   float* Ab = A + off + off * ld;
@@ -861,66 +895,6 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
       const int idx = t + 512 * i, r4 = 4 * (idx & 31), c = idx >> 5;
       *(float4*)&S[c * TLD + r4] = v[i];
     }
-  }
-  if (pre && k > 0) {
-    // A_kk -= L_{k,k-1} U_{k-1,k} on the tensor cores: mma.sync m16n8k8
-    // TF32 with the split x = hi + lo (hi = tf32(x)) and three products
-    // hi*hi + hi*lo + lo*hi (FP32-level accuracy).  Warp w owns rows
-    // 32 (w % 4) .. +31 and columns 32 (w / 4) .. +31: 2 x 4 tiles of 16 x 8.
-    const float* Lb = Ab - LU_NB * ld;  // block (k, k-1)
-    const float* Ub = Ab - LU_NB;       // block (k-1, k)
-    const int g = lane >> 2, tq = lane & 3;
-    const int rw = 32 * (warp & 3), cw = 32 * (warp >> 2);
-    float acc[2][4][4] = {};
-    for (int kc = 0; kc < LU_NB; kc += PRE_KC) {
-      __syncthreads();
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int idx = t + 512 * i, r4 = 4 * (idx & 31), q = idx >> 5;  // 32 columns of L
-        *(float4*)&Lc[q * TLD + r4] = __ldcg((const float4*)(Lb + r4 + (size_t)(kc + q) * ld));
-        const int q4 = 4 * (idx & 7), c = idx >> 3;                    // 128 columns of U
-        *(float4*)&Uc[c * PRE_ULD + q4] = __ldcg((const float4*)(Ub + kc + q4 + (size_t)c * ld));
-      }
-      __syncthreads();
-#pragma unroll
-      for (int ks = 0; ks < PRE_KC; ks += 8) {
-        uint32_t ah[2][4], al[2][4], bh[4][2], bl[4][2];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-          const int r = rw + 16 * mt + g;
-          const float av[4] = {Lc[(ks + tq) * TLD + r], Lc[(ks + tq) * TLD + r + 8], Lc[(ks + tq + 4) * TLD + r],
-                               Lc[(ks + tq + 4) * TLD + r + 8]};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) split_tf32(av[e], ah[mt][e], al[mt][e]);
-        }
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          const int c = cw + 8 * nt + g;
-          const float bv[2] = {Uc[c * PRE_ULD + ks + tq], Uc[c * PRE_ULD + ks + tq + 4]};
-#pragma unroll
-          for (int e = 0; e < 2; ++e) split_tf32(bv[e], bh[nt][e], bl[nt][e]);
-        }
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < 4; ++nt) {
-            mma_tf32_16x8x8(acc[mt][nt], al[mt], bh[nt]);
-            mma_tf32_16x8x8(acc[mt][nt], ah[mt], bl[nt]);
-            mma_tf32_16x8x8(acc[mt][nt], ah[mt], bh[nt]);
-          }
-      }
-    }
-    // accumulator layout: c0 (g, 2 tq), c1 (g, 2 tq + 1), c2 (g + 8, 2 tq), c3 (g + 8, 2 tq + 1)
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int r = rw + 16 * mt + g, c = cw + 8 * nt + 2 * tq;
-        S[c * TLD + r] -= acc[mt][nt][0];
-        S[(c + 1) * TLD + r] -= acc[mt][nt][1];
-        S[c * TLD + r + 8] -= acc[mt][nt][2];
-        S[(c + 1) * TLD + r + 8] -= acc[mt][nt][3];
-      }
   }
   __syncthreads();
   int bad = 0;
@@ -1407,11 +1381,9 @@ static float* sub_inverses(float* Dinv, int Npad, int k) {
 }
 
 // diagonal block k
-// (pre: with the update by panel k-1 of its own block, see k_diag_lu)
-static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st,
-                       int pre = 0) {
+static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st) {
   KScope kd(st, KC_LU_DIAG);
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info, pre);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info);
   count_launches(1);
 }
 
@@ -1475,9 +1447,9 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
   return (int)cudaGetLastError();
 }
 
-// Lookahead-1 schedule on three streams.  `la` (the critical path) factors
-// diagonal block k+1, applying step k's update to that block itself, then
-// its panels; `tl` meanwhile applies the rest of step k's thin update (block
+// Lookahead-1 schedule on three streams.  `la` (the critical path) applies
+// step k's update to diagonal block k+1 (one tensor-core tile), factors the
+// block, then its panels; `tl` meanwhile applies the rest of step k's thin update (block
 // column k+1 below the diagonal block and block row k+1 right of it, FP32);
 // `st` runs the bulk of step k's trailing update (its tensor-core operands
 // come from the panel kernel), and at the end forms the full inverses
@@ -1486,7 +1458,7 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
 // tc[2]: plans with separate lo/transposed buffers for even and odd steps.
 int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, cudaStream_t st,
                         cudaStream_t la, cudaEvent_t fork, cudaEvent_t* evP, cudaEvent_t* evT,
-                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err) {
+                        cudaStream_t tl, cudaEvent_t* evR, const TcPlan* tc, int* err, int* ctr) {
   const int K = Npad / LU_NB;
   lu_attrs();
   KScope total(st, KC_LU_TOTAL);
@@ -1507,7 +1479,11 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     cudaEventRecord(evR[k], tl);
     {
       KScope crit(la, KC_LU_CRIT);
-      diag_block(A, ld, Npad, Dinv, info, k + 1, la, 1);
+      // static tile order: this launch runs beside the bulk update, which
+      // owns the tile counter
+      int e = tc_gemm_sub(P, k, 0, 0, LU_NB, LU_NB, err, la);
+      if (e) return e;
+      diag_block(A, ld, Npad, Dinv, info, k + 1, la);
       cudaStreamWaitEvent(la, evR[k], 0);
       panels(A, ld, Npad, Dinv, k + 1, la, &tc[(k + 1) & 1]);
     }
@@ -1516,7 +1492,7 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     if (rem > LU_NB) {
       KScope trail(st, KC_LU_TRAIL);
       // operands Lt, Ltlo, Ulo of step k were written by its panels
-      int e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st);
+      int e = tc_gemm_sub(P, k, LU_NB, LU_NB, rem - LU_NB, rem - LU_NB, err, st, ctr);
       if (e) return e;
     }
     cudaEventRecord(evT[k], st);
@@ -1590,23 +1566,29 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const 
     cudaMemcpyAsync(out, r, sizeof(float) * Npad, cudaMemcpyDeviceToDevice, st);
     return 0;
   }
+  // CTAs per block row: as many as stay resident, at most LU_TRSV_PMAX
+  int P = max_coresident / K;
+  P = P < 1 ? 1 : (P > LU_TRSV_PMAX ? LU_TRSV_PMAX : P);
   KScope ks(st, KC_TRSV);
   count_launches(2);
   unsigned long long* t0 = tags;
   unsigned long long* t1 = tags + Npad;
+  unsigned long long* p0 = tags + 2 * (size_t)Npad;
+  unsigned long long* p1 = p0 + (size_t)LU_TRSV_PMAX * Npad;
+  const dim3 grid(K * P);
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&r, (void*)&tmp,
-                    (void*)&t0, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit, (void*)&err};
+                    (void*)&t0, (void*)&p0, (void*)&P, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit,
+                    (void*)&err};
     // forward: r -> tmp (separate output so that no CTA reads a block another rewrote)
-    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, dim3(K), dim3(256), args,
-                                                dsm, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<false>, grid, dim3(256), args, dsm, st);
     if (e != cudaSuccess) return (int)e;
   }
   {
     void* args[] = {(void*)&A, (void*)&ld, (void*)&K, (void*)&Dinv, (void*)&Mc, (void*)&tmp, (void*)&out,
-                    (void*)&t1, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit, (void*)&err};
-    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, dim3(K), dim3(256), args,
-                                                dsm, st);
+                    (void*)&t1, (void*)&p1, (void*)&P, (void*)&epoch, (void*)&wepoch, (void*)&wait_limit,
+                    (void*)&err};
+    cudaError_t e = cudaLaunchCooperativeKernel((void*)k_trsv_wave<true>, grid, dim3(256), args, dsm, st);
     if (e != cudaSuccess) return (int)e;
   }
   return 0;
@@ -1671,7 +1653,7 @@ namespace bem {
 void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float* SI, int* info,
                    cudaStream_t st) {
   lu_attrs();
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info, 0);
+  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info);
   k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1, 0, 0, 0,
                                                         nullptr, nullptr, nullptr);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);

@@ -148,7 +148,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   double* Z = (double*)c->get(bem_ctx::SLOT_LU4, sizeof(double) * (size_t)N * m);
   double* w = (double*)c->get(bem_ctx::SLOT_LU5, sizeof(double) * ((size_t)N + 64));
   float* rf = (float*)c->get(bem_ctx::SLOT_LU6, sizeof(float) * (3 * (size_t)Npad + 64) +
-                                                   sizeof(unsigned long long) * (2 * (size_t)Npad));
+                                                   sizeof(unsigned long long) * bem::lu_tag_words(Npad));
   int* info = (int*)c->get(bem_ctx::SLOT_LU7, 256);
   float* Mc = (float*)c->get(bem_ctx::SLOT_LU8, sizeof(float) * (size_t)K * 2 * LU_NB * LU_NB);
   if (!A32 || !cs || !Dinv || !V || !Z || !w || !rf || !info || !Mc) return BEM_ERR_NOMEM;
@@ -158,7 +158,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   // (epoch, value) words of the triangular sweeps; zeroed once per solve,
   // every preconditioner application uses the next epoch
   unsigned long long* tags = (unsigned long long*)(rf + 3 * (size_t)Npad + 64);
-  cudaMemsetAsync(tags, 0, sizeof(unsigned long long) * 2 * (size_t)Npad, c->stream);
+  cudaMemsetAsync(tags, 0, sizeof(unsigned long long) * bem::lu_tag_words(Npad), c->stream);
   int epoch = 0;
   int* werr = info + 1;
   SolvePin pin;
@@ -178,14 +178,16 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   const bool lookahead = use_tc && tcp[0].ok && tcp[1].ok;
   // the whole factorization as one launch sequence (equilibration, LU, block
   // inverses, sweep couplings)
+  // info[16], info[17]: tile counter of the persistent bulk updates
   auto factor = [&]() -> int {
     cudaMemsetAsync(info, 0, 2 * sizeof(int), st);
+    cudaMemsetAsync(info + 16, 0, 2 * sizeof(int), st);
     bem::lu_prepare(A64, lda, N, Npad, cs, A32, Npad, st);
     int r;
     if (lookahead)
       r = bem::lu_factor_lookahead(A32, Npad, Npad, Dinv, info, st, c->la_stream, c->fork_event,
                                    c->events.data(), c->events.data() + K, c->thin_stream,
-                                   c->events.data() + 2 * K, tcp, werr);
+                                   c->events.data() + 2 * K, tcp, werr, info + 16);
     else
       r = bem::lu_factor(A32, Npad, Npad, Dinv, info, x3, st, nullptr, werr);
     if (r) return r;
@@ -678,12 +680,13 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
     }
     k_fill_test<<<1024, 256, 0, st>>>(A1, n, n, 4242u);
     cudaMemsetAsync(info, 0, 16, st);
+    cudaMemsetAsync(info + 16, 0, 8, st);
     bem::tc_split(tcp, 0, st);
     const int rem = n - LU_NB, reps = 20;
-    for (int i = 0; i < 3; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st);
+    for (int i = 0; i < 3; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st, info + 16);
     Timer t;
     t.start(st);
-    for (int i = 0; i < reps; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st);
+    for (int i = 0; i < reps; ++i) bem::tc_gemm_sub(tcp, 0, 0, 0, rem, rem, info + 1, st, info + 16);
     t.stop(st);
     int herr = 0;
     cudaMemcpyAsync(&herr, info + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -724,6 +727,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
     float* d = (float*)(info + 8);
     float h[4];
     cudaMemsetAsync(info, 0, 16, st);
+    cudaMemsetAsync(info + 16, 0, 8, st);
     cudaMemsetAsync(d, 0, 16, st);
     for (int shape = 0; shape < 2; ++shape) {
       const int o = shape ? LU_NB : 0;
@@ -732,7 +736,7 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
       cudaMemcpyAsync(A2, A1, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, st);
       bem::tc_split(p1, 0, st);
       bem::tc_gemm_sub(p1, 0, o, o, rem - o, rem - o, info + 1, st);
-      bem::tc_gemm_sub(p2, 0, o, o, rem - o, rem - o, info + 1, st);
+      bem::tc_gemm_sub(p2, 0, o, o, rem - o, rem - o, info + 1, st, info + 16);
       k_maxdiff<<<512, 256, 0, st>>>(A1, A2, (int64_t)n * n, d + 2 * shape);
     }
     int herr = 0;
@@ -791,10 +795,11 @@ extern "C" int bem_selftest(bem_ctx* c, int which, int n, double* out) {
     return BEM_ERR_UNSUPPORTED;
   }
   Timer t1, t2;
+  cudaMemsetAsync(info + 16, 0, 8, st);
   t1.start(st);
   int rc = bem::lu_factor_lookahead(A1, n, n, Dinv, info, st, c->la_stream, c->fork_event,
                                     c->events.data(), c->events.data() + K,
-                                  c->thin_stream, c->events.data() + 2 * K, tcp, info + 1);
+                                  c->thin_stream, c->events.data() + 2 * K, tcp, info + 1, info + 16);
   t1.stop(st);
   if (rc) return c->cuda_fail((cudaError_t)rc, "selftest tcgen05 LU");
   t2.start(st);
