@@ -38,6 +38,8 @@ int ensure_workers(bem_ctx* c, int w) {
     s->opt_inject = c->opt_inject;
     s->opt_nearfield = c->opt_nearfield;
     s->opt_singular = c->opt_singular;
+    // concurrent pipelines share the SMs: one CTA per block row in the sweeps
+    s->opt_sweep_ctas = 1;
   }
   return BEM_OK;
 }

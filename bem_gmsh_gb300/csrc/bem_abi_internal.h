@@ -39,6 +39,7 @@ struct bem_ctx {
   int opt_inject = 0;              // BEM_OPT_INJECT
   int opt_nearfield = 0;           // BEM_OPT_NEARFIELD
   int opt_singular = 0;            // BEM_OPT_SINGULAR
+  int opt_sweep_ctas = 4;          // BEM_OPT_SWEEP_CTAS: CTAs per block row of the triangular sweeps
   // why the last mixed solve did not converge (MIXED_*)
   enum { MIXED_OK = 0, MIXED_PIVOT = 1, MIXED_STAGNATION = 2, MIXED_CAP = 3 };
   int mixed_fail = MIXED_OK;

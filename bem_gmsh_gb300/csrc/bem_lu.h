@@ -37,10 +37,12 @@ inline size_t lu_tag_words(int Npad) { return (size_t)(2 + 2 * LU_TRSV_PMAX) * (
 // the same tags; err: timeout flag, set when a wait polled wait_limit times
 // in vain.  wepoch_shift (failure injection, normally 0): results are
 // published under epoch + wepoch_shift, so that a nonzero shift makes every
-// dependent wait run out.  r may be clobbered.  Returns 0 or a CUDA error.
+// dependent wait run out.  pmax: at most this many CTAs per block row (the
+// count also stays within what the GPU keeps resident).  r may be clobbered.
+// Returns 0 or a CUDA error.
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st,
-                 int wait_limit = 1 << 20, int wepoch_shift = 0);
+                 int wait_limit = 1 << 20, int wepoch_shift = 0, int pmax = LU_TRSV_PMAX);
 
 void residual64(const double* A, int64_t lda, int N, const double* x, const double* b, double* r,
                 cudaStream_t st);

@@ -1545,7 +1545,7 @@ void lu_couplings(const float* A, int64_t ld, int Npad, const float* Dinv, float
 
 int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const float* Mc, float* r, float* tmp,
                  float* out, unsigned long long* tags, int epoch, int* err, cudaStream_t st, int wait_limit,
-                 int wepoch_shift) {
+                 int wepoch_shift, int pmax) {
   const int wepoch = epoch + wepoch_shift;
   const int K = Npad / LU_NB;
   static int max_coresident = 0;
@@ -1566,9 +1566,10 @@ int lu_solve_vec(const float* A, int64_t ld, int Npad, const float* Dinv, const 
     cudaMemcpyAsync(out, r, sizeof(float) * Npad, cudaMemcpyDeviceToDevice, st);
     return 0;
   }
-  // CTAs per block row: as many as stay resident, at most LU_TRSV_PMAX
+  // CTAs per block row: as many as stay resident, at most pmax
+  const int pcap = pmax < 1 ? 1 : (pmax > LU_TRSV_PMAX ? LU_TRSV_PMAX : pmax);
   int P = max_coresident / K;
-  P = P < 1 ? 1 : (P > LU_TRSV_PMAX ? LU_TRSV_PMAX : P);
+  P = P < 1 ? 1 : (P > pcap ? pcap : P);
   KScope ks(st, KC_TRSV);
   count_launches(2);
   unsigned long long* t0 = tags;

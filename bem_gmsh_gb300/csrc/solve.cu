@@ -263,7 +263,7 @@ int bem_solve_mixed_dev(bem_ctx* c, int N, const double* A64, int64_t lda, const
   auto precond = [&](const double* v, double* z) {
     bem::to_f32(v, N, Npad, rf, st);
     int e2 = bem::lu_solve_vec(A32, Npad, Npad, Dinv, Mc, rf, tmpf, outf, tags, ++epoch, werr, st,
-                               c->opt_wait_limit, (c->opt_inject & 2) ? 1 : 0);
+                               c->opt_wait_limit, (c->opt_inject & 2) ? 1 : 0, c->opt_sweep_ctas);
     if (e2) prc = e2;
     bem::from_f32_scale(outf, cs, N, z, st);
   };
@@ -609,6 +609,11 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
   if (option == BEM_OPT_NEARFIELD) {
     if (value != 0 && value != 1 && value != 5 && value != 6) return BEM_ERR_UNSUPPORTED;
     c->opt_nearfield = value;
+    return BEM_OK;
+  }
+  if (option == BEM_OPT_SWEEP_CTAS) {
+    if (value < 1 || value > bem::LU_TRSV_PMAX) return BEM_ERR_INVALID;
+    c->opt_sweep_ctas = value;
     return BEM_OK;
   }
   if (option == BEM_OPT_SINGULAR) {

@@ -78,6 +78,9 @@ extern "C" {
 #define BEM_OPT_SINGULAR 9      /* on-element rule, the reference's `singular` knob
                                    (src/Core/Assembly_full.jl:282-283): 0 (default) interpolated
                                    Guiggiani, 1 Telles cubic map of the npg Gauss rule */
+#define BEM_OPT_SWEEP_CTAS 11   /* CTAs per block row of the preconditioner's triangular sweeps (1..4, default
+                                   4; at most what the GPU keeps resident): helpers sum the block row's
+                                   earlier blocks.  Batched solves use 1 (their pipelines share the SMs). */
 #define BEM_OPT_TC_RESERVE 10   /* SMs the persistent trailing-update kernel (BEM_OPT_TCGEN05 = 2) leaves
                                    to the look-ahead's diagonal and panel kernels (default 8, <= 64) */
 
