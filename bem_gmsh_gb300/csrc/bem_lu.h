@@ -77,6 +77,8 @@ struct TcPlan {
   alignas(64) unsigned char mB[128];
   alignas(64) unsigned char mBlo[128];
   alignas(64) unsigned char mC[128];  // the matrix as C (persistent kernel)
+  alignas(64) unsigned char mB128[128];    // B and B lo with 128-column boxes
+  alignas(64) unsigned char mBlo128[128];  // (the diagonal block's own update)
   bool ok = false;
   int variant = 1;  // 1: one CTA per tile; 2: persistent, warp-specialized
   int grid = 0;     // persistent kernel: CTAs (SMs) it may use

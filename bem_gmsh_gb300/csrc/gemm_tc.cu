@@ -33,111 +33,22 @@
 
 #include "bem_lu.h"
 #include "bem_prof.h"
+#include "bem_tc.cuh"
 
 namespace bem {
 
 namespace tc {
 
-constexpr int BM = 128;
-constexpr int BN = 256;
-#define BEM_TC_BK 16
-// k chunk: one swizzle atom of FP32, 128-byte swizzle for 32, 64-byte for
-// 16, 32-byte for 8
-constexpr int BK = BEM_TC_BK;
-static_assert(BK == 32 || BK == 16 || BK == 8, "BK must be 8, 16 or 32");
-constexpr int SW_BYTES = BK * 4;           // swizzle span (bytes per row)
-constexpr int SW_SBO = 8 * SW_BYTES;       // 8-row group stride in shared memory
-constexpr uint64_t SW_LAYOUT = BK == 32 ? 2 : (BK == 16 ? 4 : 6);  // descriptor: 128B / 64B / 32B swizzle
 #define BEM_TC_STAGES 2
 #define BEM_TC_WARPS 4
 constexpr int STAGES = BEM_TC_STAGES;
 constexpr int WARPS = BEM_TC_WARPS;  // epilogue warps: 4 (all columns each) or 8 (column halves)
 constexpr int THREADS = 32 * WARPS;
-constexpr int A_BYTES = BM * BK * 4;  // 16 KB at BK = 32
-constexpr int B_BYTES = BN * BK * 4;  // 32 KB at BK = 32
-constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // hi + lo
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 static_assert(8 * (2 * STAGES + 1) + 16 <= 256, "barrier area");
 // two CTAs per SM when their shared memory fits (registers capped at 128)
 constexpr int MIN_BLOCKS = (SMEM_BYTES <= 110 * 1024 && WARPS <= 8) ? 2 : 1;
 constexpr uint32_t TMEM_COLS = 256;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-// bounded wait for the given phase parity; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  uint32_t done = 0;
-  for (int it = 0; it < (1 << 20); ++it) {
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
-                                            uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// shared-memory matrix descriptor: K-major, swizzled rows of SW_BYTES, 8-row
-// groups SW_SBO bytes apart (SBO), leading offset unused for this layout (1).
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
-  d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(SW_SBO >> 4) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  d |= SW_LAYOUT << 61;
-  return d;
-}
-
-// instruction descriptor: D f32, A/B tf32, both K-major, M=128, N=256
-constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
-
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          dtmem),
-      "l"(a), "l"(b), "r"(IDESC), "r"(accum)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-      "%30, %31}, [%32];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
-        "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]),
-        "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 struct TcArgs {
   float* C;
@@ -760,7 +671,9 @@ bool tc_plan(TcPlan& p, float* A, int64_t ld, int Npad, float* Lt, float* Ltlo, 
   p.ok = make_map((CUtensorMap*)p.mA, Lt, LU_NB, (uint64_t)Npad, LU_NB, tc::BM) &&
          make_map((CUtensorMap*)p.mAlo, Ltlo, LU_NB, (uint64_t)Npad, LU_NB, tc::BM) &&
          make_map((CUtensorMap*)p.mB, A, (uint64_t)Npad, (uint64_t)Npad, (uint64_t)ld, tc::BN) &&
-         make_map((CUtensorMap*)p.mBlo, Ulo, LU_NB, (uint64_t)Npad, LU_NB, tc::BN);
+         make_map((CUtensorMap*)p.mBlo, Ulo, LU_NB, (uint64_t)Npad, LU_NB, tc::BN) &&
+         make_map((CUtensorMap*)p.mB128, A, (uint64_t)Npad, (uint64_t)Npad, (uint64_t)ld, LU_NB) &&
+         make_map((CUtensorMap*)p.mBlo128, Ulo, LU_NB, (uint64_t)Npad, LU_NB, LU_NB);
   if (p.ok) {
     cudaFuncSetAttribute(tc::k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
   }

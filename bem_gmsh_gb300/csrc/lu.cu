@@ -17,6 +17,7 @@
 
 #include "bem_lu.h"
 #include "bem_prof.h"
+#include "bem_tc.cuh"
 #include "df32.cuh"
 
 namespace bem {
@@ -817,20 +818,38 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 //      16 x 16 block.  Column block p of L\U and both sub-block inverses are
 //      final and are written out.
 //   C  the trailing update A22 -= L21 U12 on 4 x 4 register tiles.
-// 24 block barriers in all.  In the look-ahead LU the previous step's update
-// of the block itself comes just before the kernel, as one tile of the
-// tensor-core trailing update (inside this kernel, on mma.sync, it took 12 of
-// its 45 us; the thin update leaves the block out).  70 KB of shared memory
-// and the whole register file (512 threads x 128): the kernel runs alone on
-// an SM (capped at 64 registers to share an SM with a bulk-update tile it
-// measured 40 % slower).  A and ld must allow 16-byte accesses (ld % 4 == 0,
-// 16-byte aligned A).
+// 24 block barriers in all.  In the look-ahead LU the block first gets the
+// previous step's update of itself (the thin update leaves the block out):
+// A_kk -= L_{k,k-1} U_{k-1,k} with that step's tensor-core operands, TMA
+// loads and tcgen05 MMAs into TMEM (3xTF32) while the block loads, then one
+// TMEM read per thread (the same update on mma.sync took 12 of the kernel's
+// 45 us; as a separate one-tile launch it cost a launch on the chain).  73 KB
+// of shared memory (201 KB with the update's four operand stages) and the
+// whole register file (512 threads x 128): the kernel runs alone on an SM
+// (capped at 64 registers to share an SM with a bulk-update tile it measured
+// 40 % slower).  A and ld must allow 16-byte accesses (ld % 4 == 0, 16-byte
+// aligned A).
 // ---------------------------------------------------------------------------
 constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
 // shared floats of the diagonal kernel: L\U, four double-buffered pivot
 // rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses
 constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 4 * DB * DB);
+// with the block's own update: two operand stages of the tensor-core update
+// (1024-byte aligned), their barriers and the TMEM address
+constexpr int DIAG_PRE_STAGES = 4;
+constexpr int DIAG_B_BYTES = LU_NB * tc::BK * 4;  // a 128-column B chunk
+constexpr int DIAG_STAGE_BYTES = 2 * tc::A_BYTES + 2 * DIAG_B_BYTES;
+constexpr int DIAG_SMEM_PRE = DIAG_SMEM + 1024 + DIAG_PRE_STAGES * DIAG_STAGE_BYTES + 128;
+
+// step k-1's update of diagonal block k inside k_diag_lu, A_kk -= L_{k,k-1}
+// U_{k-1,k}, from that step's tensor-core operands (the maps of its TcPlan):
+// Lt / Ltlo rows 0..127, U_{k-1,k} from the matrix at (k index, n index) =
+// (bx0, by0), Ulo columns 0..127 (B maps with 128-column boxes).
+struct DiagPre {
+  int on;
+  int bx0, by0;
+};
 
 // acc[i][j] += sum_{q in [qs, qe)} P(r0 + i, q) Q(q, c0 + j) for column-major
 // shared blocks P (P(r, q) = Pb[q * TLD + r]) and Q (Q(q, c) = Qb[c * TLD + q]);
@@ -872,8 +891,12 @@ __device__ __forceinline__ float rcp_nr(float x) {
 }
 
 __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64_t ld, int k,
-                                                 float* __restrict__ SI, int* __restrict__ info) {
-  extern __shared__ __align__(16) float dsm[];
+                                                 float* __restrict__ SI, int* __restrict__ info,
+                                                 const __grid_constant__ CUtensorMap mA,
+                                                 const __grid_constant__ CUtensorMap mAlo,
+                                                 const __grid_constant__ CUtensorMap mB,
+                                                 const __grid_constant__ CUtensorMap mBlo, DiagPre pre) {
+  extern __shared__ __align__(1024) float dsm[];
   float* S = dsm;                       // A -> L\U
   float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
   float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
@@ -882,6 +905,81 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
   const size_t off = (size_t)k * LU_NB;
   float* Ab = A + off + off * ld;
   float* SIk = SI + (size_t)k * LU_SI;  // [p][Linv_pp 256, Uinv_pp 256]
+  // the block's own update on the tensor cores: warp 0 lane 0 loads the
+  // operand chunks by TMA (four stages), warp 1 lane 0 issues the 3xTF32 MMAs
+  // into TMEM while the block itself loads into S; the product is subtracted
+  // from S below.  Every wait is bounded; a timeout sets info = -1.
+  using namespace tc;
+  uint32_t stg = 0, bars = 0, tmem = 0;
+  uint32_t* s_tmem = nullptr;
+  volatile int* s_pfail = nullptr;
+  if (pre.on) {
+    const uint32_t base_u = smem_u32(dsm);
+    const uint32_t after = base_u + (uint32_t)DIAG_SMEM;
+    stg = (after + 1023u) & ~1023u;
+    bars = stg + DIAG_PRE_STAGES * DIAG_STAGE_BYTES;  // full[4], empty[4], done
+    s_tmem = (uint32_t*)((uint8_t*)dsm + (bars - base_u) + 8 * (2 * DIAG_PRE_STAGES + 1));
+    s_pfail = (volatile int*)(s_tmem + 1);
+    if (t == 0) {
+      *s_pfail = 0;
+      for (int i = 0; i < DIAG_PRE_STAGES; ++i) {
+        mbar_init(bars + 8 * i, 1);
+        mbar_init(bars + 8 * (DIAG_PRE_STAGES + i), 1);
+      }
+      mbar_init(bars + 8 * (2 * DIAG_PRE_STAGES), 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                   "r"(LU_NB)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = *s_tmem;
+    constexpr int NCH = LU_NB / BK;
+    const uint32_t full0 = bars, empty0 = bars + 8 * DIAG_PRE_STAGES, done = bars + 8 * 2 * DIAG_PRE_STAGES;
+    if (warp == 0 && lane == 0) {
+      for (int c = 0; c < NCH; ++c) {
+        const int sidx = c % DIAG_PRE_STAGES;
+        if (c >= DIAG_PRE_STAGES && !mbar_wait(empty0 + 8 * sidx, ((c / DIAG_PRE_STAGES) - 1) & 1)) {
+          *s_pfail = 1;
+          break;
+        }
+        const uint32_t st = stg + sidx * DIAG_STAGE_BYTES;
+        mbar_expect_tx(full0 + 8 * sidx, DIAG_STAGE_BYTES);
+        tma_load_2d(st, &mA, c * BK, 0, full0 + 8 * sidx);
+        tma_load_2d(st + A_BYTES, &mAlo, c * BK, 0, full0 + 8 * sidx);
+        tma_load_2d(st + 2 * A_BYTES, &mB, pre.bx0 + c * BK, pre.by0, full0 + 8 * sidx);
+        tma_load_2d(st + 2 * A_BYTES + DIAG_B_BYTES, &mBlo, c * BK, 0, full0 + 8 * sidx);
+      }
+    } else if (warp == 1 && lane == 0) {
+      for (int c = 0; c < NCH; ++c) {
+        const int sidx = c % DIAG_PRE_STAGES;
+        if (!mbar_wait(full0 + 8 * sidx, (c / DIAG_PRE_STAGES) & 1)) {
+          *s_pfail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = stg + sidx * DIAG_STAGE_BYTES;
+        const uint64_t dah = sdesc(st), dal = sdesc(st + A_BYTES);
+        const uint64_t dbh = sdesc(st + 2 * A_BYTES), dbl = sdesc(st + 2 * A_BYTES + DIAG_B_BYTES);
+#pragma unroll
+        for (int ks = 0; ks < BK / 8; ++ks) {
+          const uint64_t o = (uint64_t)((ks * 32) >> 4);
+          const uint32_t acc0 = (c > 0 || ks > 0) ? 1u : 0u;
+          mma_tf32(tmem, dal + o, dbh + o, acc0, IDESC_N128);
+          mma_tf32(tmem, dah + o, dbl + o, 1u, IDESC_N128);
+          mma_tf32(tmem, dah + o, dbh + o, 1u, IDESC_N128);
+        }
+        mma_commit(empty0 + 8 * sidx);
+      }
+      mma_commit(done);
+    }
+    __syncwarp();
+  }
   {
     // 8 float4 per thread, all loads in flight before the first store
     float4 v[8];
@@ -897,6 +995,33 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
     }
   }
   __syncthreads();
+  if (pre.on) {
+    // S -= the product: thread (warp w, lane l) takes row 32 (w % 4) + l
+    // (its TMEM lane) and columns 32 (w / 4) .. +31
+    const uint32_t done = bars + 8 * 2 * DIAG_PRE_STAGES;
+    int ok = 0;
+    if (lane == 0) ok = mbar_wait(done, 0) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    const int all_ok = __syncthreads_and(ok) && !*s_pfail;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (all_ok) {
+      const int q = warp & 3, cb = 32 * (warp >> 2), r = 32 * q + lane;
+      uint32_t v[32];
+      tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cb, v);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) S[(cb + j) * TLD + r] -= __uint_as_float(v[j]);
+    } else if (t == 0) {
+      atomicExch(info, -1);
+      // the MMAs issued finish before their accumulator is freed
+      mbar_wait(done, 0);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(LU_NB) : "memory");
+    }
+  }
   int bad = 0;
   // phase A of panel jb (warps 0-3): factor rows jb.. of columns jb..jb+15,
   // warp 1 then inverts the unit-lower 16 x 16 block into Li
@@ -1366,7 +1491,7 @@ static void lu_attrs() {
 static void lu_attrs_once() {
   cudaFuncSetAttribute(k_diag_factor_rb, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)(sizeof(float) * LU_NB * DLD));
-  cudaFuncSetAttribute(k_diag_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
+  cudaFuncSetAttribute(k_diag_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM_PRE);
   cudaFuncSetAttribute(k_gemm_mma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)gemm_mma_smem());
   cudaFuncSetAttribute(k_gemm_mma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1380,10 +1505,23 @@ static float* sub_inverses(float* Dinv, int Npad, int k) {
   return Dinv + (size_t)(Npad / LU_NB) * 2 * LU_NB * LU_NB + (size_t)k * LU_SI;
 }
 
-// diagonal block k
-static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st) {
+// diagonal block k; with P (the plan of step k-1), the block first gets
+// that step's update on the tensor cores
+static void diag_block(float* A, int64_t ld, int Npad, float* Dinv, int* info, int k, cudaStream_t st,
+                       const TcPlan* P = nullptr) {
   KScope kd(st, KC_LU_DIAG);
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info);
+  static const CUtensorMap none{};
+  DiagPre pre{0, 0, 0};
+  const CUtensorMap* m[4] = {&none, &none, &none, &none};
+  if (P && k > 0) {
+    pre = DiagPre{1, (k - 1) * LU_NB, k * LU_NB};
+    m[0] = (const CUtensorMap*)P->mA;
+    m[1] = (const CUtensorMap*)P->mAlo;
+    m[2] = (const CUtensorMap*)P->mB128;
+    m[3] = (const CUtensorMap*)P->mBlo128;
+  }
+  k_diag_lu<<<1, 512, pre.on ? DIAG_SMEM_PRE : DIAG_SMEM, st>>>(A, ld, k, sub_inverses(Dinv, Npad, 0), info, *m[0],
+                                                              *m[1], *m[2], *m[3], pre);
   count_launches(1);
 }
 
@@ -1447,9 +1585,9 @@ int lu_factor(float* A, int64_t ld, int Npad, float* Dinv, int* info, int x3, cu
   return (int)cudaGetLastError();
 }
 
-// Lookahead-1 schedule on three streams.  `la` (the critical path) applies
-// step k's update to diagonal block k+1 (one tensor-core tile), factors the
-// block, then its panels; `tl` meanwhile applies the rest of step k's thin update (block
+// Lookahead-1 schedule on three streams.  `la` (the critical path) factors
+// diagonal block k+1 after applying step k's update to the block itself
+// (inside the diagonal kernel), then its panels; `tl` meanwhile applies the rest of step k's thin update (block
 // column k+1 below the diagonal block and block row k+1 right of it, FP32);
 // `st` runs the bulk of step k's trailing update (its tensor-core operands
 // come from the panel kernel), and at the end forms the full inverses
@@ -1479,11 +1617,7 @@ int lu_factor_lookahead(float* A, int64_t ld, int Npad, float* Dinv, int* info, 
     cudaEventRecord(evR[k], tl);
     {
       KScope crit(la, KC_LU_CRIT);
-      // static tile order: this launch runs beside the bulk update, which
-      // owns the tile counter
-      int e = tc_gemm_sub(P, k, 0, 0, LU_NB, LU_NB, err, la);
-      if (e) return e;
-      diag_block(A, ld, Npad, Dinv, info, k + 1, la);
+      diag_block(A, ld, Npad, Dinv, info, k + 1, la, &P);
       cudaStreamWaitEvent(la, evR[k], 0);
       panels(A, ld, Npad, Dinv, k + 1, la, &tc[(k + 1) & 1]);
     }
@@ -1654,7 +1788,10 @@ namespace bem {
 void diag_selftest(float* A1, float* A2, int64_t ld, float* D1, float* D2, float* SI, int* info,
                    cudaStream_t st) {
   lu_attrs();
-  k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info);
+  {
+    static const CUtensorMap none{};
+    k_diag_lu<<<1, 512, DIAG_SMEM, st>>>(A1, ld, 0, SI, info, none, none, none, none, DiagPre{0, 0, 0});
+  }
   k_panels<<<dim3(LU_NB / PW, 2), 256, PANEL_SMEM, st>>>(A1, ld, SI, D1, D1 + LU_NB * LU_NB, LU_NB, 1, 0, 0, 0,
                                                         nullptr, nullptr, nullptr);
   k_diag_factor_rb<<<1, 512, sizeof(float) * LU_NB * DLD, st>>>(A2, ld, 0, D2, info);
