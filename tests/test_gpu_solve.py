@@ -209,3 +209,58 @@ def test_full_size_solve_matches_oracle(orc):
     print(f"N = 8193: solution vs oracle {e:.2e}; rel_error GPU {ra:.12e}, oracle {rb:.12e}")
     assert e < 1e-10, e
     assert abs(ra - rb) <= 1e-10 * scale, (ra, rb)
+
+
+def test_lu_options_give_the_same_solution():
+    """The bulk-update variant, the SM reserve and the sweep CTAs per block row
+    change the schedule, not the answer: every setting reaches the FP64
+    residual floor with the same iterations, and out-of-range values are
+    rejected."""
+    from bem_gmsh_gb300 import _lib
+    ctx = _lib.Context()
+    try:
+        dad = star_domain(700, p=2, seed=5)
+        solve(dad, npg=16, mode="mixed", ctx=ctx)
+        x0 = dad.cache["x"].copy()
+        for opt, val in [(_lib.BEM_OPT_TC_RESERVE, 0), (_lib.BEM_OPT_TC_RESERVE, 24),
+                         (_lib.BEM_OPT_SWEEP_CTAS, 1), (_lib.BEM_OPT_SWEEP_CTAS, 2),
+                         (_lib.BEM_OPT_TCGEN05, 1), (_lib.BEM_OPT_TCGEN05, 0)]:
+            ctx.set_option(opt, val)
+            _, st = solve(dad, npg=16, mode="mixed", ctx=ctx, return_stats=True)
+            assert st["rel_residual"] <= 1e-14, (opt, val, st)
+            assert rel(dad.cache["x"], x0) < 1e-12, (opt, val)
+        for opt, val in [(_lib.BEM_OPT_TC_RESERVE, -1), (_lib.BEM_OPT_TC_RESERVE, 65),
+                         (_lib.BEM_OPT_SWEEP_CTAS, 0), (_lib.BEM_OPT_SWEEP_CTAS, 5), (_lib.BEM_OPT_TCGEN05, 3)]:
+            with pytest.raises(_lib.BemError):
+                ctx.set_option(opt, val)
+    finally:
+        ctx.close()
+
+
+def test_kernel_timeline():
+    """With kernel timing on, every timed launch of a mixed solve appears in
+    the timeline with its class and a non-negative duration, and the LU's
+    classes lie inside its total."""
+    from bem_gmsh_gb300 import _lib
+    ctx = _lib.Context()
+    try:
+        dad = star_domain(700, p=2, seed=6)
+        solve(dad, npg=16, mode="mixed", ctx=ctx)
+        ctx.set_option(_lib.BEM_OPT_KERNEL_TIMING, 1)
+        ctx.kernel_times()
+        ctx.kernel_trace()
+        solve(dad, npg=16, mode="mixed", ctx=ctx)
+        tr = ctx.kernel_trace()
+        ctx.set_option(_lib.BEM_OPT_KERNEL_TIMING, 0)
+        assert tr and all(b >= a for _, a, b in tr)
+        names = {c for c, _, _ in tr}
+        assert {"lu_total", "lu_diag", "lu_panels", "lu_trail", "trsv", "gemv", "far"} <= names, names
+        tot = [(a, b) for c, a, b in tr if c == "lu_total"]
+        assert len(tot) == 1
+        t0, t1 = tot[0]
+        for c, a, b in tr:
+            if c in ("lu_diag", "lu_panels", "lu_trail", "lu_thin"):
+                assert t0 - 1e-3 <= a and b <= t1 + 1e-3, (c, a, b, t0, t1)
+        assert ctx.kernel_trace() == []
+    finally:
+        ctx.close()
