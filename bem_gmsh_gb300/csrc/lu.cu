@@ -811,8 +811,9 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 //   A  warps 0-3 factor the panel: every warp holds its own copy of the 16
 //      pivot rows (lane r < 16: row jb + r) and updates them identically, and
 //      32 rows below them (lane: row jb + 16 + 32 w + lane), so no barrier
-//      is needed between columns; the pivot row of each column reaches the
-//      lanes through a double-buffered row in shared memory.  Warp 1 then
+//      is needed between columns; the pivot rows reach the lanes two at a
+//      time through a double-buffered pair of rows in shared memory (every
+//      lane forms row c+1 after column c itself).  Warp 1 then
 //      inverts the unit-lower 16 x 16 block (one column per lane).
 //   B  block row of U: U[p, >p] = Linv_pp A[p, >p]; warp 4 inverts the upper
 //      16 x 16 block.  Column block p of L\U and both sub-block inverses are
@@ -832,9 +833,10 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 // ---------------------------------------------------------------------------
 constexpr int DB = LU_SB;       // panel width
 constexpr int TLD = LU_NB + 4;  // shared leading dimension
-// shared floats of the diagonal kernel: L\U, four double-buffered pivot
-// rows, the 16 x 16 scratch of the lower inverse, the two sub-block inverses
-constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 32 + 16 * 20 + 4 * DB * DB);
+// shared floats of the diagonal kernel: L\U, four warps' double-buffered
+// pairs of pivot rows, the 16 x 16 scratch of the lower inverse, the two
+// sub-block inverses
+constexpr int DIAG_SMEM = (int)sizeof(float) * (LU_NB * TLD + 4 * 4 * DB + 16 * 20 + 4 * DB * DB);
 // with the block's own update: two operand stages of the tensor-core update
 // (1024-byte aligned), their barriers and the TMEM address
 constexpr int DIAG_PRE_STAGES = 4;
@@ -898,8 +900,8 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
                                                  const __grid_constant__ CUtensorMap mBlo, DiagPre pre) {
   extern __shared__ __align__(1024) float dsm[];
   float* S = dsm;                       // A -> L\U
-  float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][2][16]
-  float* Ls = rowbuf + 4 * 32;          // 16 x 16 unit lower, column-major, ld 20
+  float* rowbuf = S + LU_NB * TLD;      // [warp 0-3][parity][2 rows][16]
+  float* Ls = rowbuf + 4 * 4 * DB;      // 16 x 16 unit lower, column-major, ld 20
   float* LiP = Ls + 16 * 20;            // [parity][Linv_pp, Uinv_pp], column-major, ld 16
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const size_t off = (size_t)k * LU_NB;
@@ -1034,36 +1036,62 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
       PT[c] = tv ? S[(jb + c) * TLD + jb + lane] : 0.f;
       PB[c] = bv ? S[(jb + c) * TLD + rb] : 0.f;
     }
-    float* myrow = rowbuf + warp * 32;
+    // two columns per step: pivot rows c and c+1 go out together, and every
+    // lane forms row c+1 after column c itself (the same operations lane c+1
+    // performs on its own copy), so one broadcast serves two columns; the
+    // results are those of the column-by-column order
+    float* myrow = rowbuf + warp * 4 * DB;
 #pragma unroll
-    for (int c = 0; c < DB; ++c) {
-      float* rw = myrow + (c & 1) * DB;
-      if (lane == c) {
+    for (int c = 0; c < DB; c += 2) {
+      float* rw = myrow + ((c >> 1) & 1) * 2 * DB;
+      if (lane == c || lane == c + 1) {
+        float* dst = rw + (lane - c) * DB;
 #pragma unroll
         for (int q4 = 0; q4 < DB; q4 += 4)
-          *(float4*)&rw[q4] = make_float4(PT[q4], PT[q4 + 1], PT[q4 + 2], PT[q4 + 3]);
+          *(float4*)&dst[q4] = make_float4(PT[q4], PT[q4 + 1], PT[q4 + 2], PT[q4 + 3]);
       }
       __syncwarp();
-      float row[DB];
+      float r0[DB], r1[DB];
 #pragma unroll
       for (int q4 = 0; q4 < DB; q4 += 4) {
         const float4 v4 = *(const float4*)&rw[q4];
-        row[q4] = v4.x; row[q4 + 1] = v4.y; row[q4 + 2] = v4.z; row[q4 + 3] = v4.w;
+        r0[q4] = v4.x; r0[q4 + 1] = v4.y; r0[q4 + 2] = v4.z; r0[q4 + 3] = v4.w;
+        const float4 w4 = *(const float4*)&rw[DB + q4];
+        r1[q4] = w4.x; r1[q4 + 1] = w4.y; r1[q4 + 2] = w4.z; r1[q4 + 3] = w4.w;
       }
-      const float piv = row[c];
-      if (!(fabsf(piv) > 1e-30f && fabsf(piv) < INFINITY)) bad = 1;
-      const float inv = rcp_nr(piv);
+      const float p0 = r0[c];
+      if (!(fabsf(p0) > 1e-30f && fabsf(p0) < INFINITY)) bad = 1;
+      const float inv0 = rcp_nr(p0);
+      // pivot row c+1 after column c
+      {
+        const float l = r1[c] * inv0;
+#pragma unroll
+        for (int c2 = c + 1; c2 < DB; ++c2) r1[c2] = fmaf(-l, r0[c2], r1[c2]);
+      }
+      const float p1 = r1[c + 1];
+      if (!(fabsf(p1) > 1e-30f && fabsf(p1) < INFINITY)) bad = 1;
+      const float inv1 = rcp_nr(p1);
       if (lane > c && tv) {
-        const float l = PT[c] * inv;
+        const float l = PT[c] * inv0;
         PT[c] = l;
 #pragma unroll
-        for (int c2 = c + 1; c2 < DB; ++c2) PT[c2] = fmaf(-l, row[c2], PT[c2]);
+        for (int c2 = c + 1; c2 < DB; ++c2) PT[c2] = fmaf(-l, r0[c2], PT[c2]);
+      }
+      if (lane > c + 1 && tv) {
+        const float l = PT[c + 1] * inv1;
+        PT[c + 1] = l;
+#pragma unroll
+        for (int c2 = c + 2; c2 < DB; ++c2) PT[c2] = fmaf(-l, r1[c2], PT[c2]);
       }
       if (bv) {
-        const float l = PB[c] * inv;
+        const float l = PB[c] * inv0;
         PB[c] = l;
 #pragma unroll
-        for (int c2 = c + 1; c2 < DB; ++c2) PB[c2] = fmaf(-l, row[c2], PB[c2]);
+        for (int c2 = c + 1; c2 < DB; ++c2) PB[c2] = fmaf(-l, r0[c2], PB[c2]);
+        const float m = PB[c + 1] * inv1;
+        PB[c + 1] = m;
+#pragma unroll
+        for (int c2 = c + 2; c2 < DB; ++c2) PB[c2] = fmaf(-m, r1[c2], PB[c2]);
       }
     }
     if (bv) {
