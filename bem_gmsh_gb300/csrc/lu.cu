@@ -1230,7 +1230,7 @@ constexpr int PW = 32;  // slice width
 constexpr int PXLD = PW + 4;
 // shared floats of the panel kernel: the factored block, the slice, one
 // side's eight 16 x 16 sub-block inverses
-constexpr int PANEL_SMEM = (int)sizeof(float) * (LU_NB * TLD + LU_NB * PXLD + LU_SI / 2);
+constexpr int PANEL_SMEM = (int)sizeof(float) * (LU_NB * TLD + LU_NB * PXLD + LU_SI / 2 + DB * PW);
 
 __device__ __forceinline__ void cp_async16(float* dst, const float* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -1272,6 +1272,7 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
   float* Ms = psm;                   // factored block, column-major, ld TLD
   float* Xs = psm + LU_NB * TLD;     // the slice
   float* Si = Xs + LU_NB * PXLD;     // [p][16 x 16], column-major
+  float* Xp = Si + LU_SI / 2;        // the current sub-block X_p (16 x 32)
   const int t = threadIdx.x;
   const int side = blockIdx.y;
 #pragma unroll
@@ -1305,7 +1306,8 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
       const int jb = p * DB;
       const float* Li = Si + p * DB * DB;  // Linv_pp(i, q) = Li[q * 16 + i]
       {
-        // X_p = Linv_pp B_p: thread -> column t / 8, rows 2 (t % 8) .. +1
+        // X_p = Linv_pp B_p into Xp[c][16]: thread -> column t / 8, rows
+        // 2 (t % 8) .. +1
         const int c = t >> 3, r2 = 2 * (t & 7);
         float o0 = 0.f, o1 = 0.f;
 #pragma unroll
@@ -1314,11 +1316,16 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
           o0 = fmaf(Li[q * DB + r2], b, o0);
           o1 = fmaf(Li[q * DB + r2 + 1], b, o1);
         }
-        __syncthreads();
-        Xs[c * TLD + jb + r2] = o0;
-        Xs[c * TLD + jb + r2 + 1] = o1;
+        Xp[c * DB + r2] = o0;
+        Xp[c * DB + r2 + 1] = o1;
       }
       __syncthreads();
+      // rows jb.. of the slice take X_p (two values per thread)
+      {
+        const int c = t >> 3, r2 = 2 * (t & 7);
+        Xs[c * TLD + jb + r2] = Xp[c * DB + r2];
+        Xs[c * TLD + jb + r2 + 1] = Xp[c * DB + r2 + 1];
+      }
       // B_q -= L_qp X_p: thread -> row jb + 16 + (t % 128), 16 columns
       const int i = jb + DB + (t & (LU_NB - 1));
       if (i < LU_NB) {
@@ -1329,7 +1336,7 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
 #pragma unroll 4
         for (int cc = 0; cc < PW / 2; ++cc) {
           const int c = cb + cc;
-          const float* xp = Xs + c * TLD + jb;
+          const float* xp = Xp + c * DB;
           float acc = Xs[c * TLD + i];
 #pragma unroll
           for (int q4 = 0; q4 < DB; q4 += 4) {
@@ -1375,7 +1382,8 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
       const int jb = p * DB;
       const float* Ui = Si + p * DB * DB;  // Uinv_pp(q, c) = Ui[c * 16 + q]
       {
-        // X_p = B_p Uinv_pp: thread -> row t % 32, columns 2 (t / 32) .. +1
+        // X_p = B_p Uinv_pp into Xp[c][32]: thread -> row t % 32, columns
+        // 2 (t / 32) .. +1
         const int c2 = 2 * g;
         float o0 = 0.f, o1 = 0.f;
 #pragma unroll
@@ -1384,15 +1392,17 @@ __global__ void __launch_bounds__(256) k_panels(const float* __restrict__ Dk, in
           o0 = fmaf(b, Ui[c2 * DB + q], o0);
           o1 = fmaf(b, Ui[(c2 + 1) * DB + q], o1);
         }
-        __syncthreads();
-        Xs[(jb + c2) * PXLD + r] = o0;
-        Xs[(jb + c2 + 1) * PXLD + r] = o1;
+        Xp[c2 * PW + r] = o0;
+        Xp[(c2 + 1) * PW + r] = o1;
       }
       __syncthreads();
-      // B_q -= X_p U_pq: thread -> row t % 32, columns jb + 16 + t / 32 + 8 m
+      // B_q -= X_p U_pq: thread -> row t % 32, columns jb + 16 + t / 32 + 8 m;
+      // columns jb.. of the slice take X_p
       float x[DB];
 #pragma unroll
-      for (int q = 0; q < DB; ++q) x[q] = Xs[(jb + q) * PXLD + r];
+      for (int q = 0; q < DB; ++q) x[q] = Xp[q * PW + r];
+      Xs[(jb + 2 * g) * PXLD + r] = Xp[2 * g * PW + r];
+      Xs[(jb + 2 * g + 1) * PXLD + r] = Xp[(2 * g + 1) * PW + r];
       for (int c = jb + DB + g; c < LU_NB; c += 8) {
         const float* up = Ms + c * TLD + jb;
         float acc = Xs[c * PXLD + r];
