@@ -815,9 +815,10 @@ void lu_prepare(const double* A64, int64_t lda, int N, int Npad, double* cs, flo
 //      time through a double-buffered pair of rows in shared memory (every
 //      lane forms row c+1 after column c itself).  Warp 1 then
 //      inverts the unit-lower 16 x 16 block (one column per lane).
-//   B  block row of U: U[p, >p] = Linv_pp A[p, >p]; warp 4 inverts the upper
-//      16 x 16 block.  Column block p of L\U and both sub-block inverses are
-//      final and are written out.
+//   B  block row of U: U[p, >p] = Linv_pp A[p, >p].  Column block p of L\U
+//      and its lower sub-block inverse are final and are written out; warp 4
+//      inverts the upper 16 x 16 block beside the next panel's factorization
+//      (its columns of S no longer change).
 //   C  the trailing update A22 -= L21 U12 on 4 x 4 register tiles.
 // 24 block barriers in all.  In the look-ahead LU the block first gets the
 // previous step's update of itself (the thin update leaves the block out):
@@ -1154,8 +1155,7 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
   for (int p = 0; p < LU_NB / DB; ++p) {
     const int jb = p * DB;
     float* Li = LiP + (p & 1) * 2 * DB * DB;
-    float* Ui = Li + DB * DB;
-    // ---- B: block row of U, U[p, >p] = Linv_pp A[p, >p]; Uinv_pp ----
+    // ---- B: block row of U, U[p, >p] = Linv_pp A[p, >p] ----
     if (t < 128) {
       const int c = jb + DB + t;  // one thread per column
       if (c < LU_NB) {
@@ -1182,24 +1182,6 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
         for (int q4 = 0; q4 < DB; q4 += 4)
           *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
       }
-    } else if (warp == 4) {
-      // inverse of the upper 16 x 16 block, lane c < 16 solving for column
-      // c by column-oriented back substitution
-      float x[DB];
-#pragma unroll
-      for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-      for (int q = DB - 1; q >= 0; --q) {
-        const float* uc = S + (jb + q) * TLD + jb;
-        x[q] *= rcp_nr(uc[q]);
-#pragma unroll
-        for (int i = 0; i < q; ++i) x[i] = fmaf(-uc[i], x[q], x[i]);
-      }
-      if (lane < DB) {
-#pragma unroll
-        for (int i4 = 0; i4 < DB; i4 += 4)
-          *(float4*)&Ui[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
-      }
     }
     __syncthreads();
     if (warp < 4) {
@@ -1210,12 +1192,34 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
         factor_panel(jb + DB, LiP + ((p + 1) & 1) * 2 * DB * DB);
       }
     } else {
-      // ---- store column block p of L\U and its inverses; C2 ----
-      for (int idx = t - 128; idx < DB * 32; idx += 384) {
-        const int cs = jb + (idx >> 5), r4 = 4 * (idx & 31);
-        *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
+      // ---- store column block p of L\U and its lower inverse; the upper
+      // inverse (warp 4, beside the next panel's factorization); C2 ----
+      if (warp == 4) {
+        // inverse of the upper 16 x 16 block, lane c < 16 solving for column
+        // c by column-oriented back substitution; Uinv(i, c) = Ui[c * 16 + i]
+        float x[DB];
+#pragma unroll
+        for (int i = 0; i < DB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+        for (int q = DB - 1; q >= 0; --q) {
+          const float* uc = S + (jb + q) * TLD + jb;
+          x[q] *= rcp_nr(uc[q]);
+#pragma unroll
+          for (int i = 0; i < q; ++i) x[i] = fmaf(-uc[i], x[q], x[i]);
+        }
+        if (lane < DB) {
+          float* Ug = SIk + p * 2 * DB * DB + DB * DB;
+#pragma unroll
+          for (int i4 = 0; i4 < DB; i4 += 4)
+            *(float4*)&Ug[lane * DB + i4] = make_float4(x[i4], x[i4 + 1], x[i4 + 2], x[i4 + 3]);
+        }
+      } else {
+        for (int idx = t - 160; idx < DB * 32; idx += 352) {
+          const int cs = jb + (idx >> 5), r4 = 4 * (idx & 31);
+          *(float4*)(Ab + r4 + (size_t)cs * ld) = *(const float4*)&S[cs * TLD + r4];
+        }
+        for (int idx = t - 160; idx < DB * DB; idx += 352) SIk[p * 2 * DB * DB + idx] = Li[idx];
       }
-      for (int idx = t - 128; idx < 2 * DB * DB; idx += 384) SIk[p * 2 * DB * DB + idx] = Li[idx];
       if (jb + 2 * DB < LU_NB) trailing(jb, jb + 2 * DB, LU_NB, t - 128, 384);
     }
     __syncthreads();
