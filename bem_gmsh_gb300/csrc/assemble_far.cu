@@ -415,6 +415,13 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
 #pragma unroll
     for (int b = 0; b < DOF; ++b) rowsum[r][b] = 0.0;
   }
+  // FP32 H, G: the row sums in FP32 pairs (an FP64 add and conversion per
+  // entry would make GB300's FP64 pipe the kernel's bound)
+  df::f2 rs32[PREC == 0 ? SPT * DOF * DOF : 1];
+  if constexpr (PREC == 0) {
+#pragma unroll
+    for (int r = 0; r < SPT * DOF * DOF; ++r) rs32[r] = df::f2{0.f, 0.f};
+  }
 
   const size_t ld = (size_t)a.ld;
   const size_t ldg = (size_t)a.ldg;
@@ -578,7 +585,10 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
         }
 #pragma unroll
         for (int r = 0; r < SPT * DOF; ++r) {
-          rowsum[r][b] += (double)hv[b][r];
+          if constexpr (PREC == 0)
+            rs32[r * DOF + b] = df::add_f(rs32[r * DOF + b], (float)hv[b][r]);
+          else
+            rowsum[r][b] += (double)hv[b][r];
           if constexpr (FUSED) bacc[r] += (bcj == 0) ? -(double)hv[b][r] * bvj : (double)gv[b][r] * bvj;
         }
         const size_t row0 = (size_t)src0 * DOF;
@@ -637,6 +647,13 @@ __global__ void __launch_bounds__(256) far_kernel(FarArgs a) {
         rowsum[r][b] = (double)rs_df[r * DOF + b].h + (double)rs_df[r * DOF + b].l;
       bacc[r] = (double)b_df[r].h + (double)b_df[r].l;
     }
+  }
+  if constexpr (PREC == 0) {
+#pragma unroll
+    for (int r = 0; r < SPT * DOF; ++r)
+#pragma unroll
+      for (int b = 0; b < DOF; ++b)
+        rowsum[r][b] = (double)rs32[r * DOF + b].h + (double)rs32[r * DOF + b].l;
   }
   // reduce row sums across element lanes, one FP64 atomic per row
 #pragma unroll
