@@ -481,6 +481,11 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -597,27 +602,54 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     __syncthreads();
     return bad == 0;
   };
+  // the same, starting from a word loaded earlier (no round trip when its
+  // block was already published then)
+  auto fetch_pre = [&](const unsigned long long* w0, unsigned long long v) {
+    if (t < LU_NB) {
+      if ((int)(v >> 32) != epoch) {
+        const unsigned long long* w = w0 + t;
+        v = ld_acquire_u64(w);
+        int it = 0;
+        while ((int)(v >> 32) != epoch) {
+          if (++it > wait_limit) {
+            bad = 1;
+            break;
+          }
+          if (it > 8) __nanosleep(32);
+          v = ld_acquire_u64(w);
+        }
+      }
+      ys[t] = __uint_as_float((uint32_t)v);
+    }
+    __syncthreads();
+    return bad == 0;
+  };
   auto blk = [&](int s) { return UPPER ? (K - 1 - s) : s; };
   // this thread's 64 coefficients of block (b, j): row `row`, columns
   // half * 64 .. + 63 (coalesced across the warp)
   auto coef = [&](int s) { return A + (rb + row) + ((size_t)blk(s) * LU_NB + half * (LU_NB / 2)) * ld; };
   // non-adjacent blocks, two register buffers: block s+1's coefficients
-  // load while block s waits for its y and is applied
+  // and its (epoch, value) words load while block s waits for its y and is
+  // applied, so that a block published by then costs no round trip
   {
     float pa[LU_NB / 2], pb[LU_NB / 2];
+    unsigned long long ta = 0, tb = 0;
+    auto word = [&](int s) { return t < LU_NB ? ld_relaxed_u64(tags + (size_t)blk(s) * LU_NB + t) : 0ull; };
     int s = s0;
     if (s < s1) {
       const float* P0 = coef(s);
 #pragma unroll
       for (int q = 0; q < LU_NB / 2; ++q) pa[q] = P0[(size_t)q * ld];
+      ta = word(s);
     }
     while (s < s1) {
       if (s + 1 < s1) {
         const float* P1 = coef(s + 1);
 #pragma unroll
         for (int q = 0; q < LU_NB / 2; ++q) pb[q] = P1[(size_t)q * ld];
+        tb = word(s + 1);
       }
-      if (!fetch(tags + (size_t)blk(s) * LU_NB)) {
+      if (!fetch_pre(tags + (size_t)blk(s) * LU_NB, ta)) {
         if (t == 0) atomicExch(err, 1);
         return;
       }
@@ -629,8 +661,9 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
         const float* P1 = coef(s + 1);
 #pragma unroll
         for (int q = 0; q < LU_NB / 2; ++q) pa[q] = P1[(size_t)q * ld];
+        ta = word(s + 1);
       }
-      if (!fetch(tags + (size_t)blk(s) * LU_NB)) {
+      if (!fetch_pre(tags + (size_t)blk(s) * LU_NB, tb)) {
         if (t == 0) atomicExch(err, 1);
         return;
       }
