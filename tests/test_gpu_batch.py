@@ -49,3 +49,19 @@ def test_tune_batch_picks_a_candidate_and_keeps_results():
     # every domain runs the same kernels whichever worker takes it
     for a, b in zip(x_tuned, x_two):
         assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(b)
+
+
+def test_batch_matches_fp64_oracle(orc):
+    """A reduced C4 batch (uneven star domains of the C4 family, 64 to 700
+    nodes) against the FP64 oracle's assembly + LAPACK solve of each domain:
+    the refined solutions within 1e-10, the bar of the single solve."""
+    sizes = c4_sizes(8, hi=700, seed=9)
+    dads = make_batch(sizes)
+    xs, st = solve_batch(dads, npg=16, mode="mixed", nworkers=4, return_stats=True)
+    assert all(s["status"] == 0 for s in st)
+    refs = make_batch(sizes)
+    for i, ref in enumerate(refs):
+        orc.assemble(ref, npg=16)
+        orc.solve(ref)
+        xr = ref.cache["x"]
+        assert np.linalg.norm(xs[i] - xr) <= 1e-10 * np.linalg.norm(xr), (i, sizes[i])
