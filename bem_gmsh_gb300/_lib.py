@@ -25,7 +25,7 @@ BEM_OPT_NEARFIELD = 8
 BEM_OPT_SINGULAR = 9
 BEM_OPT_TC_RESERVE = 10
 BEM_OPT_SWEEP_CTAS = 11
-NEARFIELD = {"tanp3c": 0, "plain": 1, "tangent": 5, "p3c": 6}
+NEARFIELD = {"tanp3c": 0, "plain": 1, "euclid": 2, "csinh": 3, "sinhsinh": 4, "tangent": 5, "p3c": 6}
 BEM_NOALLOC_MAX_NT, BEM_NOALLOC_MAX_NE = 16384, 8192
 KERNEL_CLASSES = ["far", "near", "lu_prep", "lu_crit", "lu_trail", "trsv", "gemv", "lu_total", "lu_diag",
                   "lu_panels", "lu_thin"]

@@ -100,7 +100,8 @@ def H_G_gpu(dad: BEMdata, T=np.float32, npg: int = 20, near: str = "cpu", near_f
     near: "cpu" in the reference means near/singular entries by
     `integrate_element`; here they are computed on the GPU in FP64, so "cpu"
     and "gpu" are both accepted and give the full near correction.
-    nearfield ("tanp3c", "plain", "tangent", "p3c") and singular
+    nearfield ("tanp3c", "plain", "euclid", "csinh", "sinhsinh", "tangent",
+    "p3c") and singular
     ("guiggiani", "telles") select the near-singular map and the on-element
     rule, as the reference's cached `nearfield` and `singular` do.
     device must be "cuda" (no CPU fallback).  `out=(H, G)` may pass

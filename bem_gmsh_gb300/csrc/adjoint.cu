@@ -160,7 +160,7 @@ __device__ double near_value(const AdjArgs& a, int i, int e, const V2* nodes, V2
   ph.kind = 0;
   ph.k = a.k;
   const V2 nref{g.nx[e * nn], g.ny[e * nn]};
-  integrate_near<1>(a.R, ph, nodes, geo, pf, nref, h, gg);
+  integrate_near<1>(a.R, ph, nodes, geo, pf, g.elen[e], nref, h, gg);
   double s = 0.0;
   for (int kk = 0; kk < nn; ++kk) {
     const int j = e * nn + kk;

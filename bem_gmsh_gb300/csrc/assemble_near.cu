@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(128) near_kernel(NearArgs a) {
     double h[BEM_MAXNN * NC], gg[BEM_MAXNN * NC];
     if (near_element(pf, nodes, nn, g.elen[e], a.near_factor)) {
       V2 nref{g.nx[e * nn], g.ny[e * nn]};
-      integrate_near<NC>(a.R, a.ph, nodes, geo, pf, nref, h, gg);
+      integrate_near<NC>(a.R, a.ph, nodes, geo, pf, g.elen[e], nref, h, gg);
     } else {
       for (int k = 0; k < nn; ++k) {
         int j = e * nn + k;

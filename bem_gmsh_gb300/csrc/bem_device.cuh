@@ -5,6 +5,7 @@
 //   closest point         src/Core/Integration.jl:323-349, 1005-1033
 //   complex pole          src/Core/Integration.jl:1117-1160
 //   tanp3c map            src/Core/Integration.jl:1163-1365
+//   sinh-family maps      src/Core/Integration.jl:1062-1115, 1367-1395
 //   interpolated Guiggiani src/Core/Integration.jl:1598-1845
 //   kernels               src/Laplace/Fundamental.jl:19-25,
 //                         src/Elasticity/Fundamental.jl:28-60
@@ -33,8 +34,9 @@ struct Rules {
   int ngeo;  // CAD nodes per element, 0 = geometry from the field nodes
   int npg;   // near-field Gauss rule size
   // near-field map (`nearfield`, Integration.jl:41-93): 0 tanp3c, 1 plain
-  // Gauss, 5 tangent, 6 p3c; on-element rule (`singular`,
-  // Assembly_full.jl:282-283): 0 interpolated Guiggiani, 1 Telles
+  // Gauss, 2 euclid, 3 csinh, 4 sinhsinh, 5 tangent, 6 p3c; on-element
+  // rule (`singular`, Assembly_full.jl:282-283): 0 interpolated Guiggiani,
+  // 1 Telles
   unsigned char nearfield, singular, pad0_, pad1_;
   double leg_x[BEM_MAXNN], leg_bw[BEM_MAXNN], leg_D[BEM_MAXNN * BEM_MAXNN];
   double geo_x[BEM_MAXGEO], geo_bw[BEM_MAXGEO], geo_D[BEM_MAXGEO * BEM_MAXGEO];
@@ -311,6 +313,87 @@ __device__ inline int tanp3ctrans(const Rules& R, double z0, double e0, double* 
 }
 
 // --------------------------------------------------------------------------
+// sinh-family maps (`:euclid`, `:csinh`, `:sinhsinh`; Integration.jl:1062-1115,
+// 1367-1395).  Unlike the tangent maps these are well conditioned: a node
+// moves by b cosh(mu u - eta) per unit of its argument, the width b of the
+// peak that the node resolves, so one ulp of asinh, sinh or exp stays about
+// one ulp of the integral; they use the platform's FP64 functions.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ void sinh_consts(double a, double b, double& mu, double& eta) {
+  const double sp = asinh((1 + a) / b), sm = asinh((1 - a) / b);
+  mu = 0.5 * (sp + sm);
+  eta = 0.5 * (sp - sm);
+}
+
+// eq. (40) with a collinear real pole |z0| > 1 (_eq40_real_pole, _eq40_AB):
+// x = z0 + s exp((u - B) / A), s = -sign(z0), with x(+-1) = +-1
+static __device__ __noinline__ int eq40_real_pole(const Rules& R, double z0, double* x, double* wx) {
+  const int m = R.npg;
+  double A = 0.0, B = 0.0, s = 0.0;
+  if (fabs(z0) > 1) {
+    s = z0 > 0 ? -1.0 : 1.0;
+    const double lm = log(s * (-1 - z0)), lp = log(s * (1 - z0));
+    A = 2.0 / (lp - lm);
+    B = -A / 2 * (lp + lm);
+  }
+  if (fabs(z0) <= 1 || fabs(A) < 1e-30) {
+    for (int i = 0; i < m; ++i) { x[i] = R.qsi[i]; wx[i] = R.w[i]; }
+    return m;
+  }
+  for (int i = 0; i < m; ++i) {
+    const double e = exp((R.qsi[i] - B) / A);
+    x[i] = z0 + s * e;
+    wx[i] = R.w[i] * (s * e / A);
+  }
+  return m;
+}
+
+// _sinhtrans_iterated: niter = 1 is the sinh map about (a, b) (eq. 40),
+// niter = 2 the sinh-sinh map whose outer sinh sits on the inner one's
+// image pole; also _sinhtrans (the `:euclid` map), which is niter = 1.
+// Not inlined (nor is the `:euclid` rule below): the default tanp3c path of
+// the element integrals keeps its registers.
+static __device__ __noinline__ int sinhtrans(const Rules& R, double a, double b, int niter, double* x,
+                                             double* wx) {
+  if (fabs(b) < 1e-14 && fabs(a) > 1) return eq40_real_pole(R, a, x, wx);
+  b = fmax(b, 1e-14);
+  double ma[2], mb[2], mmu[2], meta[2];
+  int nmap = 0;
+  double aa = a, bb = b;
+  for (int it = 0; it < niter && it < 2; ++it) {
+    double mu, eta;
+    sinh_consts(aa, bb, mu, eta);
+    ma[nmap] = aa;
+    mb[nmap] = bb;
+    mmu[nmap] = mu;
+    meta[nmap] = eta;
+    ++nmap;
+    if (mu < 1e-14) break;
+    aa = fmin(fmax(eta / mu, nextafter(-1.0, 0.0)), nextafter(1.0, 0.0));
+    bb = fmax(kPi / (2 * mu), 1e-14);
+  }
+  for (int i = 0; i < R.npg; ++i) {
+    double xi = R.qsi[i], J = 1.0;
+    for (int k = nmap - 1; k >= 0; --k) {  // the last map acts on the Gauss nodes first
+      const double t = mmu[k] * xi - meta[k];
+      J *= mb[k] * mmu[k] * cosh(t);
+      xi = ma[k] + mb[k] * sinh(t);
+    }
+    x[i] = xi;
+    wx[i] = R.w[i] * J;
+  }
+  return R.npg;
+}
+
+// `:euclid`: sinh about the Euclidean closest point, width b = d / L
+static __device__ __noinline__ int euclid_rule(const Rules& R, const V2* nodes, int nn, V2 pf, double Lel,
+                                               double* x, double* wx) {
+  double a, dist;
+  closest_point_1d(R, nodes, nn, pf, a, dist);
+  return sinhtrans(R, a, fmax(dist / fmax(Lel, kEps), 1e-14), 1, x, wx);
+}
+
+// --------------------------------------------------------------------------
 // element geometry at a parent point (_shape_geom, Assembly_full.jl:608-627)
 // --------------------------------------------------------------------------
 __device__ __forceinline__ void shape_geom(const Rules& R, const V2* nodes, const V2* geo, double xi,
@@ -351,17 +434,20 @@ __device__ __forceinline__ void load_element(const GeomDev& g, int e, V2* nodes,
 // Assembly_full.jl:649-713).  h, g: [node k][component c] with NC components.
 template <int NC>
 __device__ inline void integrate_near(const Rules& R, const Physics& ph, const V2* nodes, const V2* geo,
-                               V2 pf, V2 nref, double* h, double* g) {
+                               V2 pf, double Lel, V2 nref, double* h, double* g) {
   const int nn = R.nn;
   double eta[BEM_MAXMAP], ww[BEM_MAXMAP];
   int m;
   if (R.nearfield == 1) {  // plain Gauss rule
     m = R.npg;
     for (int i = 0; i < m; ++i) { eta[i] = R.qsi[i]; ww[i] = R.w[i]; }
+  } else if (R.nearfield == 2) {
+    m = euclid_rule(R, nodes, nn, pf, Lel, eta, ww);
   } else {
     double z0, e0;
     complex_pole_1d(R, nodes, nn, pf, z0, e0);
-    if (R.nearfield == 5) m = nm::tangenttrans(R, nm::ieee(z0), nm::ieee(e0), eta, ww);
+    if (R.nearfield == 3 || R.nearfield == 4) m = sinhtrans(R, z0, e0, R.nearfield == 4 ? 2 : 1, eta, ww);
+    else if (R.nearfield == 5) m = nm::tangenttrans(R, nm::ieee(z0), nm::ieee(e0), eta, ww);
     else if (R.nearfield == 6) m = nm::p3ctrans(R, nm::ieee(z0), nm::ieee(e0), eta, ww);
     else m = tanp3ctrans(R, z0, e0, eta, ww);
   }

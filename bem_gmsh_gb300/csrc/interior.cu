@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(IT) interior_laplace_kernel(GeomDev g, Rules R
       else
         integrate_singular<1>(R, ph, nodes, geo, pf, xa, nref, h, gg);
     else
-      integrate_near<1>(R, ph, nodes, geo, pf, nref, h, gg);
+      integrate_near<1>(R, ph, nodes, geo, pf, g.elen[e], nref, h, gg);
     for (int a = 0; a < nn; ++a) {
       const int j = e * nn + a;
       gt += gg[a] * q[j] - h[a] * T[j];

@@ -607,7 +607,7 @@ extern "C" int bem_ctx_set_option(bem_ctx* c, int option, int value) {
     return BEM_OK;
   }
   if (option == BEM_OPT_NEARFIELD) {
-    if (value != 0 && value != 1 && value != 5 && value != 6) return BEM_ERR_UNSUPPORTED;
+    if (value < 0 || value > 6) return BEM_ERR_INVALID;
     c->opt_nearfield = value;
     return BEM_OK;
   }

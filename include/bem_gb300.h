@@ -73,8 +73,10 @@ extern "C" {
                                    (BEM_ERR_INTERNAL, the context stays usable) */
 #define BEM_OPT_NEARFIELD 8     /* near-singular map of the element integrals, the reference's `nearfield`
                                    knob (src/Core/Integration.jl:41-93, set per problem with set_cache!):
-                                   0 (default) tanp3c, 1 plain Gauss rule, 5 tangent (eq. 41), 6 complete
-                                   cubic p3c; the sinh-family maps return BEM_ERR_UNSUPPORTED */
+                                   0 (default) tanp3c, 1 plain Gauss rule, 2 euclid (sinh about the
+                                   closest point, b = d / L), 3 csinh (sinh on the complex pole, eq. 40),
+                                   4 sinhsinh (iterated sinh-sinh), 5 tangent (eq. 41), 6 complete cubic
+                                   p3c; other values return BEM_ERR_INVALID */
 #define BEM_OPT_SINGULAR 9      /* on-element rule, the reference's `singular` knob
                                    (src/Core/Assembly_full.jl:282-283): 0 (default) interpolated
                                    Guiggiani, 1 Telles cubic map of the npg Gauss rule */

@@ -239,12 +239,17 @@ def test_full_size_parity_every_entry(orc):
     assert gn.max() < 1e-10
 
 
-@pytest.mark.parametrize("nearfield", ["plain", "tangent", "p3c"])
+@pytest.mark.parametrize("nearfield", ["plain", "euclid", "csinh", "sinhsinh", "tangent", "p3c"])
 def test_nearfield_maps_match_oracle(orc, nearfield):
     """The reference's `nearfield` knob (src/Core/Integration.jl:41-93): the
-    plain Gauss rule and the tangent and complete-cubic maps, Laplace and
-    Kelvin, against the oracle with the same map (FP64, every entry)."""
+    plain Gauss rule, the sinh maps (about the closest point, on the complex
+    pole, iterated sinh-sinh; the straight edges' collinear poles take the
+    eq. (40) exponential branch) and the tangent and complete-cubic maps,
+    Laplace on curved quadratic and straight cubic elements (whose pole
+    comes from the closest point) and Kelvin, against the oracle with the
+    same map (FP64, every entry)."""
     for dad in (star_domain(150, p=2, seed=12, pontointerno=True),
+                quadrado(ndiv=6, ordem=3, pontointerno=True),
                 quadrado_elasticity(ndiv=9, ordem=2, props=Elasticity(1.0, 0.3, 1.0), pontointerno=True)):
         Hr, Gr = orc.assemble(dad, npg=16, nearfield=nearfield, store=False)
         H, G = H_G_gpu(dad, T=np.float64, npg=16, nearfield=nearfield, store=False)

@@ -230,7 +230,8 @@ def test_lu_options_give_the_same_solution():
             assert st["rel_residual"] <= 1e-14, (opt, val, st)
             assert rel(dad.cache["x"], x0) < 1e-12, (opt, val)
         for opt, val in [(_lib.BEM_OPT_TC_RESERVE, -1), (_lib.BEM_OPT_TC_RESERVE, 65),
-                         (_lib.BEM_OPT_SWEEP_CTAS, 0), (_lib.BEM_OPT_SWEEP_CTAS, 5), (_lib.BEM_OPT_TCGEN05, 3)]:
+                         (_lib.BEM_OPT_SWEEP_CTAS, 0), (_lib.BEM_OPT_SWEEP_CTAS, 5), (_lib.BEM_OPT_TCGEN05, 3),
+                         (_lib.BEM_OPT_NEARFIELD, 7), (_lib.BEM_OPT_NEARFIELD, -1)]:
             with pytest.raises(_lib.BemError):
                 ctx.set_option(opt, val)
     finally:
