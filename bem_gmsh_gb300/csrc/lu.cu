@@ -628,13 +628,31 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
   // this thread's 64 coefficients of block (b, j): row `row`, columns
   // half * 64 .. + 63 (coalesced across the warp)
   auto coef = [&](int s) { return A + (rb + row) + ((size_t)blk(s) * LU_NB + half * (LU_NB / 2)) * ld; };
+  // the helpers' partial sums, loaded by the owner together with its last
+  // non-adjacent block (the helpers' shares end earlier, so these words are
+  // usually published by then and the owner's dependent step loses the
+  // round trip it spent polling them one after another)
+  unsigned long long pwv[LU_TRSV_PMAX - 1];
+#pragma unroll
+  for (int q = 0; q < LU_TRSV_PMAX - 1; ++q) pwv[q] = 0;
+  auto pre_parts = [&]() {
+    if (owner && t < LU_NB) {
+#pragma unroll
+      for (int q = 0; q < LU_TRSV_PMAX - 1; ++q)
+        if (q + 1 < P) pwv[q] = ld_relaxed_u64(ptags + (size_t)(b * P + q) * LU_NB + t);
+    }
+  };
   // non-adjacent blocks, two register buffers: block s+1's coefficients
   // and its (epoch, value) words load while block s waits for its y and is
   // applied, so that a block published by then costs no round trip
   {
     float pa[LU_NB / 2], pb[LU_NB / 2];
     unsigned long long ta = 0, tb = 0;
-    auto word = [&](int s) { return t < LU_NB ? ld_relaxed_u64(tags + (size_t)blk(s) * LU_NB + t) : 0ull; };
+    auto word = [&](int s) {
+      if (s == s1 - 1) pre_parts();
+      return t < LU_NB ? ld_relaxed_u64(tags + (size_t)blk(s) * LU_NB + t) : 0ull;
+    };
+    if (s0 == s1) pre_parts();
     int s = s0;
     if (s < s1) {
       const float* P0 = coef(s);
@@ -683,8 +701,10 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const float* __restrict__ A, 
     return;
   }
   float sum = (t < LU_NB) ? part[0][t] + part[1][t] : 0.f;
-  for (int q = 0; q + 1 < P; ++q) {
-    if (!fetch(ptags + (size_t)(b * P + q) * LU_NB)) {
+#pragma unroll
+  for (int q = 0; q < LU_TRSV_PMAX - 1; ++q) {
+    if (q + 1 >= P) break;
+    if (!fetch_pre(ptags + (size_t)(b * P + q) * LU_NB, pwv[q])) {
       if (t == 0) atomicExch(err, 1);
       return;
     }
