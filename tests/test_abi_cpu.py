@@ -91,3 +91,16 @@ def test_python_constants_match_header_defines():
     defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+(BEM_[A-Z0-9_]+)\s+(\d+)\b", txt)}
     for name in ("BEM_NOALLOC_MAX_NT", "BEM_NOALLOC_MAX_NE"):
         assert getattr(_lib, name) == defines[name], name
+    # every option, status and kind constant the binding defines has the header's value
+    named = [n for n in defines if hasattr(_lib, n)]
+    assert sum(n.startswith("BEM_OPT_") for n in named) >= 11, named
+    for name in named:
+        assert getattr(_lib, name) == defines[name], name
+
+
+def test_nearfield_codes_match_the_oracle():
+    """The near-field map names of the binding carry the codes the oracle
+    uses for the same maps (the GPU parity tests pass one name to both)."""
+    from bem_gmsh_gb300 import _lib
+    from oracle import oracle as orc
+    assert _lib.NEARFIELD == orc.NEARFIELD
