@@ -300,10 +300,14 @@ def kirsch_static(r, theta, a=1.0, sigma_inf=1.0):
     return srr, stt, srt
 
 
-def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib.Context | None = None):
+def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib.Context | None = None,
+                     nearfield: str = "tanp3c", singular: str = "guiggiani"):
     """Laplace potential at interior points from the solved boundary data
     (`interior_laplace`, src/Laplace/Lubrication.jl:399-416): every element
-    integrated with the near-field quadrature, T(p) = (g.q - h.T) / c."""
+    integrated with the near-field quadrature, T(p) = (g.q - h.T) / c.
+    nearfield and singular select the near-singular map (the problem's
+    cached `nearfield`) and the rule for points on an element, as in
+    `H_G_gpu`."""
     if not isinstance(dad.properties, Laplace):
         raise ValueError("interior_laplace needs a Laplace problem")
     if T is None or q is None:
@@ -316,8 +320,9 @@ def interior_laplace(dad: BEMdata, pts, npg: int = 16, T=None, q=None, ctx: _lib
     out = np.zeros(len(pts))
     ctx = ctx or _lib.default_context()
     g, keep = geom_struct(dad, device=False)
-    rc = ctx.L.bem_interior_laplace2d(ctx.h, g, float(dad.properties.k), int(npg), _ptr(T), _ptr(q),
-                                      len(pts), _ptr(xp), _ptr(yp), _lib.BEM_MEM_HOST, _ptr(out))
+    with _rules(ctx, nearfield, singular):
+        rc = ctx.L.bem_interior_laplace2d(ctx.h, g, float(dad.properties.k), int(npg), _ptr(T), _ptr(q),
+                                          len(pts), _ptr(xp), _ptr(yp), _lib.BEM_MEM_HOST, _ptr(out))
     ctx.check(rc, "interior_laplace")
     return out
 

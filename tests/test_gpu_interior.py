@@ -31,6 +31,24 @@ def test_interior_matches_oracle(orc):
     assert np.mean(err <= 1e-13) > 0.9
 
 
+@pytest.mark.parametrize("nearfield", ["euclid", "csinh", "sinhsinh", "plain"])
+def test_interior_with_other_near_maps_matches_oracle(orc, nearfield):
+    """The near-field map chosen by the problem's `nearfield` also drives the
+    interior integrals (src/Laplace/Lubrication.jl:399-416 through
+    `transform`): the GPU and the oracle with the same map, points down to
+    1e-3 from the boundary."""
+    dad = star_domain(200, p=2, seed=9)
+    orc.assemble(dad, npg=16)
+    orc.solve(dad)
+    T, q = dad.cache["T"], dad.cache["q"]
+    pts = np.concatenate([internal_grid(dad, 8, 8), [[0.0, 0.0]], 0.999 * dad.collocation[::37]])
+    ref = orc.interior_laplace(dad, pts, npg=16, nearfield=nearfield, T=T, q=q)
+    got = interior_laplace(dad, pts, npg=16, T=T, q=q, nearfield=nearfield)
+    err = np.abs(got - ref) / np.max(np.abs(ref))
+    print(f"interior {nearfield}: max {err.max():.2e} of the largest value")
+    assert np.all(err <= 1e-11), err.max()
+
+
 def test_interior_approach_gpu():
     """test/laplace.jl:55-86 (tanp3c): |T(0.5, d) - 0.5| < 5e-3, d -> 1e-6."""
     dad = quadrado(ndiv=20, pontointerno=False)
