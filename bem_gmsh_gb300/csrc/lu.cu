@@ -1208,33 +1208,31 @@ __global__ void __launch_bounds__(512, 1) k_diag_lu(float* __restrict__ A, int64
   for (int p = 0; p < LU_NB / DB; ++p) {
     const int jb = p * DB;
     float* Li = LiP + (p & 1) * 2 * DB * DB;
-    // ---- B: block row of U, U[p, >p] = Linv_pp A[p, >p] ----
-    if (t < 128) {
-      const int c = jb + DB + t;  // one thread per column
-      if (c < LU_NB) {
-        float v[DB], o[DB];
+    // ---- B: block row of U, U[p, >p] = Linv_pp A[p, >p]: four threads
+    // per column (lanes 4m .. 4m+3 of one warp), rows 4 (t % 4) .. +3 each;
+    // the column is read whole before any of its four threads writes ----
+    {
+      const int c = jb + DB + (t >> 2), i0 = 4 * (t & 3);
+      const bool on = c < LU_NB;
+      float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+      if (on) {
+        float v[DB];
 #pragma unroll
         for (int q4 = 0; q4 < DB; q4 += 4) {
           const float4 a = *(const float4*)&S[c * TLD + jb + q4];
           v[q4] = a.x; v[q4 + 1] = a.y; v[q4 + 2] = a.z; v[q4 + 3] = a.w;
         }
 #pragma unroll
-        for (int i = 0; i < DB; ++i) o[i] = 0.f;
-#pragma unroll
         for (int q = 0; q < DB; ++q) {
-#pragma unroll
-          for (int i4 = 0; i4 < DB; i4 += 4) {
-            const float4 l = *(const float4*)&Li[q * DB + i4];
-            o[i4] = fmaf(l.x, v[q], o[i4]);
-            o[i4 + 1] = fmaf(l.y, v[q], o[i4 + 1]);
-            o[i4 + 2] = fmaf(l.z, v[q], o[i4 + 2]);
-            o[i4 + 3] = fmaf(l.w, v[q], o[i4 + 3]);
-          }
+          const float4 l = *(const float4*)&Li[q * DB + i0];
+          o0 = fmaf(l.x, v[q], o0);
+          o1 = fmaf(l.y, v[q], o1);
+          o2 = fmaf(l.z, v[q], o2);
+          o3 = fmaf(l.w, v[q], o3);
         }
-#pragma unroll
-        for (int q4 = 0; q4 < DB; q4 += 4)
-          *(float4*)&S[c * TLD + jb + q4] = make_float4(o[q4], o[q4 + 1], o[q4 + 2], o[q4 + 3]);
       }
+      __syncwarp();
+      if (on) *(float4*)&S[c * TLD + jb + i0] = make_float4(o0, o1, o2, o3);
     }
     __syncthreads();
     if (warp < 4) {
