@@ -31,7 +31,7 @@ struct bem_ctx {
   Buf slots[NSLOT];
   int pair_cap_hint = 0;
   int opt_tcgen05 = 2;  // BEM_OPT_TCGEN05: trailing updates on tcgen05 (2: persistent kernel)
-  int opt_tc_reserve = 8;  // BEM_OPT_TC_RESERVE: SMs the persistent kernel leaves free
+  int opt_tc_reserve = 0;  // BEM_OPT_TC_RESERVE: SMs the persistent kernel leaves free
   int opt_far_df = 1;   // BEM_OPT_FAR_DF
   int opt_graphs = 1;   // BEM_OPT_GRAPHS
   int opt_pivot_fallback = 1;      // BEM_OPT_PIVOT_FALLBACK

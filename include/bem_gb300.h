@@ -84,7 +84,7 @@ extern "C" {
                                    4; at most what the GPU keeps resident): helpers sum the block row's
                                    earlier blocks.  Batched solves use 1 (their pipelines share the SMs). */
 #define BEM_OPT_TC_RESERVE 10   /* SMs the persistent trailing-update kernel (BEM_OPT_TCGEN05 = 2) leaves
-                                   to the look-ahead's diagonal and panel kernels (default 8, <= 64) */
+                                   to the look-ahead's diagonal and panel kernels (default 0, <= 64) */
 
 /* kernel classes reported by bem_kernel_times */
 #define BEM_KC_FAR 0       /* far-field tile kernel of the assembly */
