@@ -104,3 +104,16 @@ def test_nearfield_codes_match_the_oracle():
     from bem_gmsh_gb300 import _lib
     from oracle import oracle as orc
     assert _lib.NEARFIELD == orc.NEARFIELD
+
+
+def test_quadrature_knobs_rejected_on_the_host():
+    """Names outside the built maps and rules (the anisotropic `:zsinh`, a
+    misspelt rule) raise before any device call, as the reference's
+    `transform` / `H_G_gpu` reject them."""
+    from bem_gmsh_gb300.api import _rules
+    with pytest.raises(ValueError):
+        _rules(None, "zsinh", "guiggiani")
+    with pytest.raises(ValueError):
+        _rules(None, "tanp3c", "gauss")
+    r = _rules(None, "sinhsinh", "telles")
+    assert (r.nf, r.sg) == (4, 1)
